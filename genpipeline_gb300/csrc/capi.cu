@@ -1,0 +1,163 @@
+// capi.cu -- context, error state and element stiffness of the gbsimp C ABI.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "internal.h"
+
+namespace gbs {
+
+static thread_local char g_err[512] = "";
+
+int set_error(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof g_err, fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int cuda_error(cudaError_t e, const char *what) {
+    return set_error(GBS_ECUDA, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+static const int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                  {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+
+// B^T D B summed over the 2x2x2 Gauss points of the unit cube. The integrand is
+// polynomial of degree <= 2 per axis, so the two-point rule is exact.
+static void ke_quadrature(double nu, double e0, double *ke) {
+    const double lam = e0 * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    const double mu = e0 / (2.0 * (1.0 + nu));
+    const double g[2] = {0.5 - 0.5 / sqrt(3.0), 0.5 + 0.5 / sqrt(3.0)};
+    memset(ke, 0, 576 * sizeof(double));
+    for (int q = 0; q < 8; ++q) {
+        const double gx = g[q & 1], gy = g[(q >> 1) & 1], gz = g[(q >> 2) & 1];
+        // grad N_a at the point, and the six strains (xx, yy, zz, xy, yz, zx) per DOF.
+        double B[6][24];
+        memset(B, 0, sizeof B);
+        for (int a = 0; a < 8; ++a) {
+            const double sx = kCorner[a][0] ? 1.0 : -1.0, sy = kCorner[a][1] ? 1.0 : -1.0,
+                         sz = kCorner[a][2] ? 1.0 : -1.0;
+            const double fx = kCorner[a][0] ? gx : 1.0 - gx, fy = kCorner[a][1] ? gy : 1.0 - gy,
+                         fz = kCorner[a][2] ? gz : 1.0 - gz;
+            const double dNx = sx * fy * fz, dNy = fx * sy * fz, dNz = fx * fy * sz;
+            B[0][3 * a + 0] = dNx;
+            B[1][3 * a + 1] = dNy;
+            B[2][3 * a + 2] = dNz;
+            B[3][3 * a + 0] = dNy;
+            B[3][3 * a + 1] = dNx;
+            B[4][3 * a + 1] = dNz;
+            B[4][3 * a + 2] = dNy;
+            B[5][3 * a + 0] = dNz;
+            B[5][3 * a + 2] = dNx;
+        }
+        // D B with the isotropic D (lam + 2 mu on the normal diagonal, mu for shears).
+        double DB[6][24];
+        for (int c = 0; c < 24; ++c) {
+            const double tr = B[0][c] + B[1][c] + B[2][c];
+            for (int m = 0; m < 3; ++m) DB[m][c] = lam * tr + 2.0 * mu * B[m][c];
+            for (int m = 3; m < 6; ++m) DB[m][c] = mu * B[m][c];
+        }
+        for (int r = 0; r < 24; ++r)
+            for (int c = 0; c < 24; ++c) {
+                double s = 0.0;
+                for (int m = 0; m < 6; ++m) s += B[m][r] * DB[m][c];
+                ke[r * 24 + c] += s * 0.125;
+            }
+    }
+    for (int r = 0; r < 24; ++r)
+        for (int c = r + 1; c < 24; ++c) {
+            const double s = 0.5 * (ke[r * 24 + c] + ke[c * 24 + r]);
+            ke[r * 24 + c] = ke[c * 24 + r] = s;
+        }
+}
+
+void *thread_pinned() {
+    // One small pinned buffer per host thread, so that threads sharing a context never
+    // share a staging buffer. It lives until the process exits.
+    static thread_local void *buf = nullptr;
+    if (!buf && cudaMallocHost(&buf, 4096) != cudaSuccess) buf = nullptr;
+    return buf;
+}
+
+static void install_ke(gbsimp_ctx *ctx, const double *ke) {
+    double mx = 0.0, tr = 0.0;
+    for (int i = 0; i < 576; ++i) {
+        ctx->ke[i] = ke[i];
+        ctx->kef.k[i] = (float)ke[i];
+        ctx->ked.k[i] = ke[i];
+        mx = fmax(mx, fabs(ke[i]));
+    }
+    // Rigid translations in the kernel of Ke: sum over the 8 nodes of column block c.
+    for (int r = 0; r < 24; ++r)
+        for (int c = 0; c < 3; ++c) {
+            double s = 0.0;
+            for (int b = 0; b < 8; ++b) s += ke[r * 24 + 3 * b + c];
+            tr = fmax(tr, fabs(s));
+        }
+    ctx->translation_free = mx > 0.0 && tr <= 1e-12 * mx;
+    for (int i = 0; i < 24; ++i) {
+        ctx->ke_diag_d[i] = ke[i * 25];
+        ctx->ke_diag_f[i] = (float)ke[i * 25];
+    }
+}
+
+}  // namespace gbs
+
+using namespace gbs;
+
+extern "C" int gbsimp_abi_version(void) { return GBSIMP_ABI_VERSION; }
+
+extern "C" const char *gbsimp_last_error(void) { return g_err; }
+
+extern "C" int gbsimp_ke_quadrature(double nu, double e0, double *ke576) {
+    if (!ke576 || !(nu > -1.0 && nu < 0.5) || !(e0 > 0.0))
+        return set_error(GBS_EINVAL, "gbsimp_ke_quadrature: need -1 < nu < 0.5, e0 > 0");
+    ke_quadrature(nu, e0, ke576);
+    return GBS_OK;
+}
+
+extern "C" int gbsimp_create(gbsimp_ctx **out) {
+    if (!out) return set_error(GBS_EINVAL, "gbsimp_create: null out");
+    *out = nullptr;
+    gbsimp_ctx *c = (gbsimp_ctx *)calloc(1, sizeof(gbsimp_ctx));
+    if (!c) return set_error(GBS_ENOMEM, "gbsimp_create: out of host memory");
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e != cudaSuccess) {
+        free(c);
+        return cuda_error(e, "cudaGetDevice");
+    }
+    e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (e != cudaSuccess) {
+        free(c);
+        return cuda_error(e, "cudaDeviceGetAttribute");
+    }
+    double ke[576];
+    ke_quadrature(0.3, 1.0, ke);
+    install_ke(c, ke);
+    *out = c;
+    return GBS_OK;
+}
+
+extern "C" int gbsimp_destroy(gbsimp_ctx *ctx) {
+    if (!ctx) return GBS_OK;
+    free(ctx);
+    return GBS_OK;
+}
+
+extern "C" int gbsimp_set_ke(gbsimp_ctx *ctx, const double *ke576) {
+    if (!ctx || !ke576) return set_error(GBS_EINVAL, "gbsimp_set_ke: bad arguments");
+    for (int i = 0; i < 576; ++i)
+        if (!isfinite(ke576[i])) return set_error(GBS_EINVAL, "gbsimp_set_ke: non-finite entry %d", i);
+    install_ke(ctx, ke576);
+    return GBS_OK;
+}
+
+extern "C" int gbsimp_get_ke(const gbsimp_ctx *ctx, double *ke576) {
+    if (!ctx || !ke576) return set_error(GBS_EINVAL, "gbsimp_get_ke: bad arguments");
+    memcpy(ke576, ctx->ke, sizeof ctx->ke);
+    return GBS_OK;
+}

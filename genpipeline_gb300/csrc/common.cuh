@@ -1,0 +1,151 @@
+// common.cuh -- shared definitions of the gbsimp CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gbsimp.h"
+
+namespace gbs {
+
+// Element-local node a sits at corner (cx, cy, cz) of its element; reference order of
+// genpipeline/topology/simp_solver.py:256-266.
+__host__ __device__ constexpr int corner_x(int a) { return (a == 1 || a == 2 || a == 5 || a == 6) ? 1 : 0; }
+__host__ __device__ constexpr int corner_y(int a) { return (a == 2 || a == 3 || a == 6 || a == 7) ? 1 : 0; }
+__host__ __device__ constexpr int corner_z(int a) { return a >= 4 ? 1 : 0; }
+
+// Element stiffness passed BY VALUE as a kernel parameter: kernel parameters live in a
+// constant bank, so with fully unrolled loops every Ke entry is an FFMA/DFMA operand read
+// straight from the constant cache, with no load instruction and no shared memory.
+struct KeF {
+    float k[576];
+};
+struct KeD {
+    double k[576];
+};
+
+// Stiffness law (gbsimp_law) in the arithmetic type of a kernel.
+template <typename T>
+struct Law {
+    int kind;  // 0 ref: e0*max(x,xmin)^p ; 1 modified: emin + x^p (e0-emin)
+    int pint;  // penal when it is an integer 1..4, else -1
+    T penal, e0, emin, xmin;
+};
+
+template <typename T>
+Law<T> make_law(const gbsimp_law &l) {
+    Law<T> r;
+    r.kind = l.kind;
+    r.penal = (T)l.penal;
+    r.e0 = (T)l.e0;
+    r.emin = (T)l.emin;
+    r.xmin = (T)l.xmin;
+    r.pint = -1;
+    for (int i = 1; i <= 4; ++i)
+        if (l.penal == (double)i) r.pint = i;
+    return r;
+}
+
+// x^n for n in 0..4 by multiplication, else pow(x, p).
+__device__ __forceinline__ double powp(double x, int n, double p) {
+    switch (n) {
+        case 0: return 1.0;
+        case 1: return x;
+        case 2: return x * x;
+        case 3: return x * x * x;
+        case 4: return (x * x) * (x * x);
+        default: return pow(x, p);
+    }
+}
+__device__ __forceinline__ float powp(float x, int n, float p) {
+    switch (n) {
+        case 0: return 1.0f;
+        case 1: return x;
+        case 2: return x * x;
+        case 3: return x * x * x;
+        case 4: return (x * x) * (x * x);
+        default: return powf(x, p);
+    }
+}
+
+// E(x) of one element.
+template <typename T>
+__device__ __forceinline__ T modulus(const Law<T> &L, T x) {
+    if (L.kind == 0) {
+        T xm = x > L.xmin ? x : L.xmin;
+        return L.e0 * powp(xm, L.pint, L.penal);
+    }
+    return L.emin + powp(x, L.pint, L.penal) * (L.e0 - L.emin);
+}
+
+// dE/dx of one element; law 0 evaluates it at the floored density, as the reference does
+// (simp_solver.py:218).
+template <typename T>
+__device__ __forceinline__ T dmodulus(const Law<T> &L, T x) {
+    const int n1 = L.pint >= 1 ? L.pint - 1 : -1;
+    if (L.kind == 0) {
+        T xm = x > L.xmin ? x : L.xmin;
+        return L.e0 * L.penal * powp(xm, n1, L.penal - (T)1);
+    }
+    return L.penal * powp(x, n1, L.penal - (T)1) * (L.e0 - L.emin);
+}
+
+// Warp / block sums in FP64 (fixed shuffle order => deterministic).
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Sums v over the block; the result is valid in thread 0. scratch: >= 32 doubles.
+__device__ __forceinline__ double block_sum(double v, double *scratch) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) scratch[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (warp == 0) {
+        r = lane < nw ? scratch[lane] : 0.0;
+        r = warp_sum(r);
+    }
+    return r;
+}
+
+}  // namespace gbs
+
+// ---- library-internal host helpers (capi.cu) -------------------------------------------
+struct gbsimp_ctx {
+    int device;
+    double ke[576];
+    gbs::KeF kef;
+    gbs::KeD ked;
+    bool translation_free;  // Ke annihilates rigid translations (quadrature Ke: yes)
+    float ke_diag_f[24];
+    double ke_diag_d[24];
+    int num_sms;
+};
+
+namespace gbs {
+int set_error(int code, const char *fmt, ...);
+int cuda_error(cudaError_t e, const char *what);
+}  // namespace gbs
+
+#define GBS_CUDA_TRY(call)                                           \
+    do {                                                             \
+        cudaError_t _e = (call);                                     \
+        if (_e != cudaSuccess) return gbs::cuda_error(_e, #call);    \
+    } while (0)
+
+#define GBS_LAUNCH_CHECK(what)                                       \
+    do {                                                             \
+        cudaError_t _e = cudaGetLastError();                         \
+        if (_e != cudaSuccess) return gbs::cuda_error(_e, what);     \
+    } while (0)

@@ -1,0 +1,495 @@
+// elem.cu -- element-wise kernels: sensitivity/compliance, density filter, OC bisection,
+// FP64 dot. All reductions: per-block FP64 partials, summed in block order by the last
+// block to finish (deterministic for a given launch shape).
+#include <math.h>
+#include <string.h>
+
+#include "internal.h"
+
+namespace gbs {
+
+// ---- last-block reduction helper -----------------------------------------------------
+// Every block calls it with its partial(s); returns true in the last block, whose threads
+// then see the K sums of all partials in out[0..K-1] (shared). counter is reset.
+template <int K>
+__device__ bool last_block_reduce(const double (&v)[K], double *partials, unsigned *counter, double *out,
+                                  double *sred) {
+    __shared__ bool last;
+    const int nblk = gridDim.x;
+    double bs[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) bs[k] = block_sum(v[k], sred);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) partials[k * nblk + blockIdx.x] = bs[k];
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == (unsigned)(nblk - 1));
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double s = 0.0;
+        for (int i = threadIdx.x; i < nblk; i += blockDim.x) s += ((volatile double *)partials)[k * nblk + i];
+        s = block_sum(s, sred);
+        if (threadIdx.x == 0) out[k] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *counter = 0;
+    return true;
+}
+
+inline unsigned reduce_blocks(const gbsimp_ctx *ctx, int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    const int64_t cap = 4LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+// ---- sensitivity ------------------------------------------------------------------------
+// Thread per element: u_e gathered in FP64 (minus node 0's displacement when Ke annihilates
+// translations), ce = u_e^T Ke u_e, dc = -dE/dx ce, energy partial E ce.
+__global__ void __launch_bounds__(128) sens_kernel(int nx, int ny, int nz, Law<double> law, const KeD ke, int sub,
+                                                   const float *__restrict__ x, const double *__restrict__ u,
+                                                   float *dc, float *ce_out, double *partials, unsigned *counter,
+                                                   double *energy_out) {
+    __shared__ double sred[32];
+    __shared__ double tot[1];
+    const int64_t n_elem = (int64_t)nx * ny * nz;
+    const int64_t NY = ny + 1, NZ = nz + 1;
+    double part = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_elem; e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e / ((int64_t)ny * nz)), j = (int)((e / nz) % ny), k = (int)(e % nz);
+        double ue[24];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            const int64_t m = ((int64_t)(i + corner_x(b)) * NY + (j + corner_y(b))) * NZ + (k + corner_z(b));
+#pragma unroll
+            for (int c = 0; c < 3; ++c) ue[3 * b + c] = u[3 * m + c];
+        }
+        if (sub) {
+            const double c0 = ue[0], c1 = ue[1], c2 = ue[2];
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                ue[3 * b] -= c0;
+                ue[3 * b + 1] -= c1;
+                ue[3 * b + 2] -= c2;
+            }
+        }
+        double s = 0.0;
+#pragma unroll
+        for (int r = 0; r < 24; ++r) {
+            double t = 0.0;
+#pragma unroll
+            for (int q = 0; q < 24; ++q) t = fma(ke.k[r * 24 + q], ue[q], t);
+            s = fma(ue[r], t, s);
+        }
+        const double xe = (double)x[e];
+        if (dc) dc[e] = (float)(-dmodulus(law, xe) * s);
+        if (ce_out) ce_out[e] = (float)s;
+        part += modulus(law, xe) * s;
+    }
+    if (energy_out) {
+        const double v[1] = {part};
+        if (last_block_reduce<1>(v, partials, counter, tot, sred) && threadIdx.x == 0) *energy_out = tot[0];
+    }
+}
+
+// ---- density filter ---------------------------------------------------------------------
+constexpr int kMaxStencil = 1024;
+struct Stencil {
+    int n;
+    int r;
+    int off[kMaxStencil];  // dx, dy, dz packed as signed bytes
+    float w[kMaxStencil];  // rmin - dist > 0
+};
+
+// The neighbourhood of simp_solver.py:1553-1565: offsets of the box of half-width
+// ceil(rmin) with dist <= rmin; zero weights (dist == rmin) are dropped (they add nothing).
+static int make_stencil(double rmin, Stencil *s) {
+    if (!(rmin > 0.0) || rmin > 6.0) return set_error(GBS_EINVAL, "filter: rmin must be in (0, 6], got %g", rmin);
+    const int r = (int)ceil(rmin);
+    s->n = 0;
+    s->r = r;
+    for (int di = -r; di <= r; ++di)
+        for (int dj = -r; dj <= r; ++dj)
+            for (int dk = -r; dk <= r; ++dk) {
+                const double d = sqrt((double)(di * di + dj * dj + dk * dk));
+                if (d > rmin) continue;
+                const double w = rmin - d;
+                if (!(w > 0.0)) continue;
+                if (s->n >= kMaxStencil) return set_error(GBS_EINVAL, "filter: stencil too large");
+                s->off[s->n] = (int)(((unsigned)(uint8_t)(int8_t)di) | ((unsigned)(uint8_t)(int8_t)dj << 8) |
+                                     ((unsigned)(uint8_t)(int8_t)dk << 16));
+                s->w[s->n] = (float)w;
+                ++s->n;
+            }
+    return GBS_OK;
+}
+
+__device__ __forceinline__ void unpack_off(int o, int &di, int &dj, int &dk) {
+    di = (int)(int8_t)(o & 0xff);
+    dj = (int)(int8_t)((o >> 8) & 0xff);
+    dk = (int)(int8_t)((o >> 16) & 0xff);
+}
+
+// mode 0: out = (sum w v) / hs[e] (hs nullable: computed);  mode 1: out = sum w v/hs[e2];
+// mode 2 (hs): out = sum w over in-bounds neighbours. preserved (mode 0): out = 1 there.
+__global__ void __launch_bounds__(256) filter_kernel(int nx, int ny, int nz, const Stencil st, int mode,
+                                                     const float *__restrict__ hs, const float *__restrict__ in,
+                                                     const uint8_t *__restrict__ preserved, float *out) {
+    const int64_t n_elem = (int64_t)nx * ny * nz;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_elem; e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e / ((int64_t)ny * nz)), j = (int)((e / nz) % ny), k = (int)(e % nz);
+        double s = 0.0, ws = 0.0;
+        for (int q = 0; q < st.n; ++q) {
+            int di, dj, dk;
+            unpack_off(st.off[q], di, dj, dk);
+            const int i2 = i + di, j2 = j + dj, k2 = k + dk;
+            if (i2 < 0 || i2 >= nx || j2 < 0 || j2 >= ny || k2 < 0 || k2 >= nz) continue;
+            const int64_t e2 = ((int64_t)i2 * ny + j2) * nz + k2;
+            const double w = (double)st.w[q];
+            ws += w;
+            if (mode == 0) s += w * (double)in[e2];
+            else if (mode == 1) s += w * ((double)in[e2] / (double)hs[e2]);
+        }
+        float o;
+        if (mode == 0) {
+            const double h = hs ? (double)hs[e] : ws;
+            o = (float)(s / h);
+            if (preserved && preserved[e]) o = 1.0f;
+        } else if (mode == 1) {
+            o = (float)s;
+        } else {
+            o = (float)ws;
+        }
+        out[e] = o;
+    }
+}
+
+static unsigned elem_blocks(const gbsimp_ctx *ctx, int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    const int64_t cap = 32LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+    if (b > cap) b = cap;
+    return (unsigned)(b < 1 ? 1 : b);
+}
+
+int filter_launch(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, int mode, const float *hs,
+                  const float *in, const uint8_t *preserved, float *out, cudaStream_t st) {
+    Stencil s;
+    int rc = make_stencil(rmin, &s);
+    if (rc) return rc;
+    const int64_t n = (int64_t)nx * ny * nz;
+    filter_kernel<<<elem_blocks(ctx, n, 256), 256, 0, st>>>(nx, ny, nz, s, mode, hs, in, preserved, out);
+    GBS_LAUNCH_CHECK("filter_kernel");
+    return GBS_OK;
+}
+
+// ---- OC bisection -----------------------------------------------------------------------
+struct OcScalars {
+    double l1, l2, lfinal, npres;
+    int steps, done;
+    unsigned counter;
+    int pad;
+};
+
+struct OcParams {
+    float move, sqrt_floor;
+    double tol, tol_eps, volfrac, l1, l2;
+    int max_bisect;
+};
+
+// Workspace: [OcScalars (256 B)] [hs: n floats] [w: n floats] [partials: 4*cap doubles]
+struct OcWs {
+    OcScalars *sc;
+    float *hs, *w;
+    double *partials;
+};
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static size_t oc_ws_bytes(int64_t n) {
+    return 256 + 2 * align256((size_t)n * sizeof(float)) + align256(4 * 4096 * sizeof(double));
+}
+
+static OcWs oc_ws(void *ws, int64_t n) {
+    char *p = (char *)ws;
+    OcWs w;
+    w.sc = (OcScalars *)p;
+    p += 256;
+    w.hs = (float *)p;
+    p += align256((size_t)n * sizeof(float));
+    w.w = (float *)p;
+    p += align256((size_t)n * sizeof(float));
+    w.partials = (double *)p;
+    return w;
+}
+
+// w_e = sum_{e1 in ball(e), e1 not preserved} H[e1,e] / Hs[e1];  npres = #preserved.
+__global__ void oc_weights_kernel(int nx, int ny, int nz, const Stencil st, const float *__restrict__ hs,
+                                  const uint8_t *__restrict__ preserved, float *w, double *partials, OcScalars *sc) {
+    __shared__ double sred[32];
+    __shared__ double tot[1];
+    const int64_t n_elem = (int64_t)nx * ny * nz;
+    double np = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_elem; e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e / ((int64_t)ny * nz)), j = (int)((e / nz) % ny), k = (int)(e % nz);
+        double s = 0.0;
+        for (int q = 0; q < st.n; ++q) {
+            int di, dj, dk;
+            unpack_off(st.off[q], di, dj, dk);
+            const int i2 = i + di, j2 = j + dj, k2 = k + dk;
+            if (i2 < 0 || i2 >= nx || j2 < 0 || j2 >= ny || k2 < 0 || k2 >= nz) continue;
+            const int64_t e2 = ((int64_t)i2 * ny + j2) * nz + k2;
+            if (preserved && preserved[e2]) continue;
+            s += (double)st.w[q] / (double)hs[e2];
+        }
+        w[e] = (float)s;
+        if (preserved && preserved[e]) np += 1.0;
+    }
+    const double v[1] = {np};
+    if (last_block_reduce<1>(v, partials, &sc->counter, tot, sred) && threadIdx.x == 0) sc->npres = tot[0];
+}
+
+__device__ __forceinline__ float oc_trial(float x, float dc, float inv_l, const OcParams &P, bool pres) {
+    float t = -dc * inv_l;
+    t = t > P.sqrt_floor ? t : P.sqrt_floor;
+    float v = x * sqrtf(t);
+    v = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+    const float lo = x - P.move, hi = x + P.move;
+    v = v < lo ? lo : v;
+    v = v > hi ? hi : v;
+    return pres ? 1.0f : v;
+}
+
+__global__ void oc_init_kernel(int64_t n, const OcParams P, const float *__restrict__ dc, double *partials,
+                               OcScalars *sc) {
+    __shared__ double sred[32];
+    __shared__ double tot[1];
+    sc->done = 0;  // every block writes the same values
+    sc->steps = 0;
+    if (P.l2 >= 0.0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            sc->l1 = P.l1;
+            sc->l2 = P.l2;
+            sc->lfinal = 0.5 * (P.l1 + P.l2);
+        }
+        return;
+    }
+    // l2 = 2 * max(max(-dc), 1)  (simp_solver_gpu.py:813); max via a sum of per-block maxima
+    // would lose the max, so partials carry maxima and the last block takes their max.
+    float m = -INFINITY;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, -dc[e]);
+    m = warp_max(m);
+    __shared__ float wm[32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) wm[wid] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float b = -INFINITY;
+        for (int i = 0; i < (int)((blockDim.x + 31) >> 5); ++i) b = fmaxf(b, wm[i]);
+        partials[blockIdx.x] = (double)b;
+        __threadfence();
+        last = (atomicAdd(&sc->counter, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    (void)sred;
+    (void)tot;
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double mm = -INFINITY;
+        for (unsigned i = 0; i < gridDim.x; ++i) mm = fmax(mm, ((volatile double *)partials)[i]);
+        sc->counter = 0;
+        sc->l1 = P.l1;
+        sc->l2 = 2.0 * (mm > 1.0 ? mm : 1.0);
+        sc->lfinal = 0.5 * (sc->l1 + sc->l2);
+    }
+}
+
+// One bisection step (simp_solver.py:229-247). Every block evaluates the same tolerance
+// test on (l1, l2); when it holds, the step only records lfinal.
+__global__ void __launch_bounds__(256) oc_step_kernel(int64_t n, const OcParams P, const float *__restrict__ x,
+                                                      const float *__restrict__ dc, const uint8_t *__restrict__ pres,
+                                                      const float *__restrict__ w, double *partials,
+                                                      OcScalars *sc) {
+    __shared__ double sred[32];
+    __shared__ double tot[1];
+    if (sc->done) return;
+    const double l1 = sc->l1, l2 = sc->l2;
+    const double lmid = 0.5 * (l2 + l1);
+    if ((l2 - l1) / (l1 + l2 + P.tol_eps) < P.tol) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            sc->lfinal = lmid;
+            sc->steps += 1;
+            sc->done = 1;
+        }
+        return;
+    }
+    const float inv_l = (float)(1.0 / lmid);
+    double v = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        const bool pr = pres && pres[e];
+        if (pr) continue;
+        v += (double)w[e] * (double)oc_trial(x[e], dc[e], inv_l, P, false);
+    }
+    const double vv[1] = {v};
+    if (last_block_reduce<1>(vv, partials, &sc->counter, tot, sred) && threadIdx.x == 0) {
+        const double vol = (tot[0] + sc->npres) / (double)n;
+        if (vol > P.volfrac)
+            sc->l1 = lmid;
+        else
+            sc->l2 = lmid;
+        sc->lfinal = lmid;
+        sc->steps += 1;
+        if (sc->steps >= P.max_bisect) sc->done = 1;
+    }
+}
+
+__global__ void oc_final_kernel(int64_t n, const OcParams P, const float *__restrict__ x,
+                                const float *__restrict__ dc, const uint8_t *__restrict__ pres, const OcScalars *sc,
+                                float *xnew) {
+    const float inv_l = (float)(1.0 / sc->lfinal);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        xnew[e] = oc_trial(x[e], dc[e], inv_l, P, pres && pres[e]);
+}
+
+// ---- FP64 dot ---------------------------------------------------------------------------
+__global__ void dot_f64_kernel(int64_t n, const double *__restrict__ a, const double *__restrict__ b,
+                               double *partials, unsigned *counter, double *out) {
+    __shared__ double sred[32];
+    __shared__ double tot[1];
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s = fma(a[i], b[i], s);
+    const double v[1] = {s};
+    if (last_block_reduce<1>(v, partials, counter, tot, sred) && threadIdx.x == 0) *out = tot[0];
+}
+
+}  // namespace gbs
+
+using namespace gbs;
+
+// ---- C ABI ------------------------------------------------------------------------------
+static size_t reduce_ws_bytes(int64_t nblocks) { return 256 + ((size_t)nblocks * 8 * 4 + 255) / 256 * 256; }
+
+extern "C" size_t gbsimp_sensitivity_ws_bytes(int nx, int ny, int nz) {
+    (void)nx;
+    (void)ny;
+    (void)nz;
+    return reduce_ws_bytes(4096);
+}
+
+extern "C" int gbsimp_sensitivity(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
+                                  const double *u, float *dc, float *ce, double *energy_out, void *ws,
+                                  size_t ws_bytes, void *stream) {
+    if (!ctx || !law || !x || !u || nx <= 0 || ny <= 0 || nz <= 0)
+        return set_error(GBS_EINVAL, "gbsimp_sensitivity: bad arguments");
+    if (energy_out && (!ws || ws_bytes < gbsimp_sensitivity_ws_bytes(nx, ny, nz)))
+        return set_error(GBS_EINVAL, "gbsimp_sensitivity: workspace too small");
+    const int64_t n = (int64_t)nx * ny * nz;
+    const unsigned blocks = reduce_blocks(ctx, n, 128);
+    unsigned *counter = (unsigned *)ws;
+    double *partials = (double *)((char *)ws + 256);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (energy_out) GBS_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
+    sens_kernel<<<blocks, 128, 0, st>>>(nx, ny, nz, make_law<double>(*law), ctx->ked, ctx->translation_free ? 1 : 0, x,
+                                        u, dc, ce, partials, counter, energy_out);
+    GBS_LAUNCH_CHECK("sens_kernel");
+    return GBS_OK;
+}
+
+extern "C" int gbsimp_filter_hs(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, float *hs, void *stream) {
+    if (!ctx || !hs || nx <= 0 || ny <= 0 || nz <= 0) return set_error(GBS_EINVAL, "gbsimp_filter_hs: bad arguments");
+    return filter_launch(ctx, nx, ny, nz, rmin, 2, nullptr, nullptr, nullptr, hs, (cudaStream_t)stream);
+}
+
+extern "C" int gbsimp_filter(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const float *hs, const float *in,
+                             float *out, int transpose, void *stream) {
+    if (!ctx || !in || !out || nx <= 0 || ny <= 0 || nz <= 0)
+        return set_error(GBS_EINVAL, "gbsimp_filter: bad arguments");
+    if (transpose && !hs) return set_error(GBS_EINVAL, "gbsimp_filter: the transpose needs hs");
+    return filter_launch(ctx, nx, ny, nz, rmin, transpose ? 1 : 0, hs, in, nullptr, out, (cudaStream_t)stream);
+}
+
+extern "C" size_t gbsimp_oc_ws_bytes(int nx, int ny, int nz) { return oc_ws_bytes((int64_t)nx * ny * nz); }
+
+extern "C" int gbsimp_oc_prepare(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const uint8_t *preserved,
+                                 void *ws, size_t ws_bytes, void *stream) {
+    if (!ctx || nx <= 0 || ny <= 0 || nz <= 0 || !ws) return set_error(GBS_EINVAL, "gbsimp_oc_prepare: bad arguments");
+    const int64_t n = (int64_t)nx * ny * nz;
+    if (ws_bytes < oc_ws_bytes(n)) return set_error(GBS_EINVAL, "gbsimp_oc_prepare: workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    OcWs w = oc_ws(ws, n);
+    GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(OcScalars), st));
+    int rc = filter_launch(ctx, nx, ny, nz, rmin, 2, nullptr, nullptr, nullptr, w.hs, st);
+    if (rc) return rc;
+    Stencil s;
+    rc = make_stencil(rmin, &s);
+    if (rc) return rc;
+    oc_weights_kernel<<<reduce_blocks(ctx, n, 256), 256, 0, st>>>(nx, ny, nz, s, w.hs, preserved, w.w, w.partials, w.sc);
+    GBS_LAUNCH_CHECK("oc_weights_kernel");
+    return GBS_OK;
+}
+
+extern "C" int gbsimp_oc(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const gbsimp_oc_params *prm,
+                         const float *x, const float *dc, const uint8_t *preserved, float *xnew, float *xphys,
+                         void *ws, size_t ws_bytes, void *stream) {
+    if (!ctx || !prm || !x || !dc || !xnew || !xphys || !ws || nx <= 0 || ny <= 0 || nz <= 0)
+        return set_error(GBS_EINVAL, "gbsimp_oc: bad arguments");
+    const int64_t n = (int64_t)nx * ny * nz;
+    if (ws_bytes < oc_ws_bytes(n)) return set_error(GBS_EINVAL, "gbsimp_oc: workspace too small");
+    if (prm->max_bisect <= 0 || prm->max_bisect > 1000) return set_error(GBS_EINVAL, "gbsimp_oc: max_bisect out of range");
+    if (x == xnew) return set_error(GBS_EINVAL, "gbsimp_oc: x and xnew must not alias");
+    cudaStream_t st = (cudaStream_t)stream;
+    OcWs w = oc_ws(ws, n);
+    OcParams P;
+    P.move = (float)prm->move;
+    P.sqrt_floor = (float)prm->sqrt_floor;
+    P.tol = prm->tol;
+    P.tol_eps = prm->tol_eps;
+    P.volfrac = prm->volfrac;
+    P.l1 = prm->l1;
+    P.l2 = prm->l2;
+    P.max_bisect = prm->max_bisect;
+    const unsigned blocks = reduce_blocks(ctx, n, 256);
+    oc_init_kernel<<<blocks, 256, 0, st>>>(n, P, dc, w.partials, w.sc);
+    GBS_LAUNCH_CHECK("oc_init_kernel");
+    for (int k = 0; k < prm->max_bisect; ++k) {
+        oc_step_kernel<<<blocks, 256, 0, st>>>(n, P, x, dc, preserved, w.w, w.partials, w.sc);
+        GBS_LAUNCH_CHECK("oc_step_kernel");
+    }
+    oc_final_kernel<<<elem_blocks(ctx, n, 256), 256, 0, st>>>(n, P, x, dc, preserved, w.sc, xnew);
+    GBS_LAUNCH_CHECK("oc_final_kernel");
+    return filter_launch(ctx, nx, ny, nz, rmin, 0, w.hs, xnew, preserved, xphys, st);
+}
+
+extern "C" int gbsimp_oc_result(gbsimp_ctx *ctx, const void *ws, double *lambda_out, int *steps_out, void *stream) {
+    if (!ctx || !ws) return set_error(GBS_EINVAL, "gbsimp_oc_result: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    OcScalars h;
+    void *hp = thread_pinned();
+    if (!hp) return set_error(GBS_ECUDA, "gbsimp_oc_result: no pinned staging buffer");
+    GBS_CUDA_TRY(cudaMemcpyAsync(hp, ws, sizeof(OcScalars), cudaMemcpyDeviceToHost, st));
+    GBS_CUDA_TRY(cudaStreamSynchronize(st));
+    memcpy(&h, hp, sizeof h);
+    if (lambda_out) *lambda_out = h.lfinal;
+    if (steps_out) *steps_out = h.steps;
+    return GBS_OK;
+}
+
+extern "C" int gbsimp_dot_f64(gbsimp_ctx *ctx, int64_t n, const double *a, const double *b, double *out, void *ws,
+                              size_t ws_bytes, void *stream) {
+    if (!ctx || !a || !b || !out || !ws || n < 0) return set_error(GBS_EINVAL, "gbsimp_dot_f64: bad arguments");
+    if (ws_bytes < reduce_ws_bytes(4096)) return set_error(GBS_EINVAL, "gbsimp_dot_f64: workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned *counter = (unsigned *)ws;
+    double *partials = (double *)((char *)ws + 256);
+    GBS_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
+    dot_f64_kernel<<<reduce_blocks(ctx, n, 256), 256, 0, st>>>(n, a, b, partials, counter, out);
+    GBS_LAUNCH_CHECK("dot_f64_kernel");
+    return GBS_OK;
+}

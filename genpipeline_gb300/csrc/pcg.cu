@@ -1,0 +1,674 @@
+// pcg.cu -- Jacobi-PCG drivers: FP32 matrix-free PCG, FP32-inner / FP64-outer defect
+// correction, and a CSR PCG for the pcg_solve_cuda contract.
+//
+// One PCG iteration k is two launches (after setup r_0, z_0 = r_0/diag, p_{-1} = 0):
+//   K1  apply_tile_kernel<MODE_PCG>: p_k = z_k + beta_k p_{k-1} on the halo while staging,
+//       x += alpha_{k-1} p_{k-1} on owned nodes, Ap_k = D K D p_k, p_k.Ap_k -> alpha_k.
+//   K2  pcg_update_kernel: r_{k+1} = r_k - alpha_k Ap_k, ||r||^2 and r.z -> beta_{k+1},
+//       the stop test ||r|| < rtol ||D b|| (simp_solver_gpu.py:328-379).
+// Every scalar lives on the device; each kernel exits at once when the solve is done, so
+// the host can launch whole chunks of iterations and look at the status once per chunk.
+#include <math.h>
+#include <string.h>
+
+#include <chrono>
+
+#include "apply_tile.cuh"
+#include "internal.h"
+
+namespace gbs {
+
+static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static inline int64_t n_dof_of(int nx, int ny, int nz) { return 3LL * (nx + 1) * (ny + 1) * (nz + 1); }
+
+static inline unsigned vec_blocks(const gbsimp_ctx *ctx, int64_t n) {
+    int64_t b = (n + 255) / 256;
+    const int64_t cap = 4LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+    if (b > cap) b = cap;
+    return (unsigned)(b < 1 ? 1 : b);
+}
+
+// ---- workspace of the FP32 PCG -----------------------------------------------------------
+struct PcgWs {
+    PcgScalars *sc;
+    float *r, *dinv, *p0, *p1, *ap;
+    double *partials;
+    size_t partial_count;
+};
+
+static size_t pcg_partials(int nx, int ny, int nz) {
+    const dim3 g = tile_grid<TileF>(nx, ny, nz);
+    size_t n = (size_t)g.x * g.y * g.z;
+    return n > 3 * 4096 ? n : 3 * 4096;
+}
+
+static size_t pcg_ws_bytes_impl(int nx, int ny, int nz) {
+    const size_t nd = (size_t)n_dof_of(nx, ny, nz);
+    return al256(sizeof(PcgScalars)) + 5 * al256(nd * sizeof(float)) + al256(pcg_partials(nx, ny, nz) * sizeof(double));
+}
+
+static PcgWs pcg_ws(void *ws, int nx, int ny, int nz) {
+    const size_t nd = (size_t)n_dof_of(nx, ny, nz);
+    char *p = (char *)ws;
+    PcgWs w;
+    w.sc = (PcgScalars *)p;
+    p += al256(sizeof(PcgScalars));
+    float **v[5] = {&w.r, &w.dinv, &w.p0, &w.p1, &w.ap};
+    for (int i = 0; i < 5; ++i) {
+        *v[i] = (float *)p;
+        p += al256(nd * sizeof(float));
+    }
+    w.partials = (double *)p;
+    w.partial_count = pcg_partials(nx, ny, nz);
+    return w;
+}
+
+__device__ __forceinline__ bool dof_fixed(const uint8_t *mask, int64_t d) {
+    return mask && ((mask[d / 3] >> (int)(d % 3)) & 1);
+}
+
+// dinv = 1 / diag(K(x)) on free DOFs, 0 on fixed DOFs; diag_{n,c} = sum_{e ∋ n} E_e Ke[(a,c),(a,c)].
+template <typename T>
+__global__ void dinv_kernel(int nx, int ny, int nz, Law<T> law, const KeF kd, const float *__restrict__ x,
+                            const uint8_t *__restrict__ mask, float *dinv) {
+    const int64_t NY = ny + 1, NZ = nz + 1;
+    const int64_t n_nodes = (int64_t)(nx + 1) * NY * NZ;
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(n / (NY * NZ)), j = (int)((n / NZ) % NY), k = (int)(n % NZ);
+        T acc[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            const int ei = i - corner_x(a), ej = j - corner_y(a), ek = k - corner_z(a);
+            if (ei < 0 || ej < 0 || ek < 0 || ei >= nx || ej >= ny || ek >= nz) continue;
+            const T E = modulus(law, (T)x[((int64_t)ei * ny + ej) * nz + ek]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) acc[c] += E * (T)kd.k[(3 * a + c) * 25];
+        }
+        const uint8_t m = mask ? mask[n] : (uint8_t)0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) dinv[3 * n + c] = ((m >> c) & 1) || !(acc[c] > 0) ? 0.0f : (float)(1.0 / (double)acc[c]);
+    }
+}
+
+// Block sums of three quantities; the last block finishes the reduction.
+__device__ bool last_block3(double a, double b, double c, double *partials, unsigned *counter, double *out) {
+    __shared__ double sred[32];
+    __shared__ bool last;
+    const int nblk = gridDim.x;
+    const double ba = block_sum(a, sred);
+    const double bb = block_sum(b, sred);
+    const double bc = block_sum(c, sred);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = ba;
+        partials[nblk + blockIdx.x] = bb;
+        partials[2 * nblk + blockIdx.x] = bc;
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == (unsigned)(nblk - 1));
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    for (int k = 0; k < 3; ++k) {
+        double s = 0.0;
+        for (int i = threadIdx.x; i < nblk; i += blockDim.x) s += ((volatile double *)partials)[k * nblk + i];
+        s = block_sum(s, sred);
+        if (threadIdx.x == 0) out[k] = s;
+    }
+    if (threadIdx.x == 0) *counter = 0;
+    return true;
+}
+
+// r = D b - q (q = D K D x0), x0 fixed entries zeroed, p_{-1} = 0; sums r.z, r.r, (Db).(Db).
+__global__ void pcg_init_kernel(int64_t nd, const float *__restrict__ b, const float *__restrict__ q,
+                                const uint8_t *__restrict__ mask, const float *__restrict__ dinv, float *r, float *pprev,
+                                float *xu, double *partials, PcgScalars *sc, double tol, int max_iter) {
+    double rz = 0.0, rr = 0.0, bb = 0.0;
+    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
+        const bool fx = dof_fixed(mask, d);
+        const float bd = fx ? 0.0f : b[d];
+        const float rd = fx ? 0.0f : bd - q[d];
+        r[d] = rd;
+        pprev[d] = 0.0f;
+        if (fx) xu[d] = 0.0f;
+        rz += (double)rd * (double)rd * (double)dinv[d];
+        rr += (double)rd * (double)rd;
+        bb += (double)bd * (double)bd;
+    }
+    __shared__ double tot[3];
+    if (last_block3(rz, rr, bb, partials, &sc->counter, tot) && threadIdx.x == 0) {
+        sc->rz = tot[0];
+        sc->rr = tot[1];
+        sc->bnorm = sqrt(tot[2]);
+        sc->alpha[0] = sc->alpha[1] = 0.0;
+        sc->beta = 0.0;
+        sc->tol = tol;
+        sc->pap = 0.0;
+        sc->iter = 0;
+        sc->max_iter = max_iter;
+        sc->status = GBS_OK;
+        const bool fin = isfinite(tot[0]) && isfinite(tot[1]) && isfinite(tot[2]);
+        sc->done = (!fin || sc->bnorm == 0.0 || sqrt(tot[1]) < tol * sc->bnorm || max_iter <= 0) ? 1 : 0;
+        if (!fin) sc->status = GBS_ENONFINITE;
+        else if (max_iter <= 0 && !(sqrt(tot[1]) < tol * sc->bnorm) && sc->bnorm != 0.0) sc->status = GBS_ENOTCONV;
+    }
+}
+
+__global__ void __launch_bounds__(256) pcg_update_kernel(int64_t nd, const float *__restrict__ ap,
+                                                         const float *__restrict__ dinv, float *r, double *partials,
+                                                         PcgScalars *sc) {
+    if (sc->done) return;
+    const int it = sc->iter;
+    const float alpha = (float)sc->alpha[it & 1];
+    double rz = 0.0, rr = 0.0;
+    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
+        const float rd = fmaf(-alpha, ap[d], r[d]);
+        r[d] = rd;
+        rr += (double)rd * (double)rd;
+        rz += (double)rd * (double)rd * (double)dinv[d];
+    }
+    __shared__ double tot[3];
+    if (last_block3(rz, rr, 0.0, partials, &sc->counter, tot) && threadIdx.x == 0) {
+        sc->iter = it + 1;
+        sc->rr = tot[1];
+        if (!isfinite(tot[0]) || !isfinite(tot[1])) {
+            sc->done = 1;
+            sc->status = GBS_ENONFINITE;
+        } else if (sqrt(tot[1]) < sc->tol * sc->bnorm) {
+            sc->done = 1;
+        } else if (it + 1 >= sc->max_iter) {
+            sc->done = 1;
+            sc->status = GBS_ENOTCONV;
+        }
+        sc->beta = tot[0] / sc->rz;
+        sc->rz = tot[0];
+    }
+}
+
+// x += alpha_last p_last after the loop (the iteration that met the stop test has not yet
+// added its own step), or x = 0 when D b = 0.
+__global__ void pcg_finalize_kernel(int64_t nd, const float *p0, const float *p1, float *xu, const PcgScalars *sc) {
+    const int st = sc->status;
+    const int it = sc->iter;
+    const bool zero = sc->bnorm == 0.0;
+    if (!zero && (it == 0 || st == GBS_EBREAKDOWN || st == GBS_ENONFINITE)) return;
+    const float alpha = (float)sc->alpha[(it - 1) & 1];
+    const float *p = ((it - 1) & 1) ? p1 : p0;
+    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x)
+        xu[d] = zero ? 0.0f : fmaf(alpha, p[d], xu[d]);
+}
+
+static int read_scalars(const PcgScalars *d, PcgScalars *h, cudaStream_t st) {
+    void *hp = thread_pinned();
+    if (!hp) return set_error(GBS_ECUDA, "no pinned staging buffer");
+    GBS_CUDA_TRY(cudaMemcpyAsync(hp, d, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
+    GBS_CUDA_TRY(cudaStreamSynchronize(st));
+    memcpy(h, hp, sizeof(PcgScalars));
+    return GBS_OK;
+}
+
+// Launches one K1+K2 iteration.
+static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
+                         const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st) {
+    TileArgs<float> A{nx, ny, nz, x, nullptr, w.ap, mask};
+    PcgArgs pa{w.r, w.dinv, w.p0, w.p1, u, w.partials, w.sc};
+    const dim3 g = tile_grid<TileF>(nx, ny, nz), b = tile_block<TileF>();
+    if (ctx->translation_free)
+        apply_tile_kernel<float, KeF, TileF::X, TileF::Y, TileF::Z, true, MODE_PCG><<<g, b, 0, st>>>(A, law, ctx->kef, pa);
+    else
+        apply_tile_kernel<float, KeF, TileF::X, TileF::Y, TileF::Z, false, MODE_PCG><<<g, b, 0, st>>>(A, law, ctx->kef, pa);
+    GBS_LAUNCH_CHECK("apply_tile_kernel<PCG>");
+    const int64_t nd = n_dof_of(nx, ny, nz);
+    pcg_update_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.ap, w.dinv, w.r, w.partials, w.sc);
+    GBS_LAUNCH_CHECK("pcg_update_kernel");
+    return GBS_OK;
+}
+
+// FP32 PCG. u: x0 in, solution out. Returns GBS_OK and fills *out (status inside).
+int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x, const float *b,
+            const uint8_t *mask, float *u, double rtol, int max_iter, int check_every, void *ws, PcgScalars *out,
+            cudaStream_t st) {
+    const int64_t nd = n_dof_of(nx, ny, nz);
+    PcgWs w = pcg_ws(ws, nx, ny, nz);
+    const Law<float> law = make_law<float>(*glaw);
+    GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
+    dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, law, ctx->kef, x, mask, w.dinv);
+    GBS_LAUNCH_CHECK("dinv_kernel");
+    int rc = apply_f32(ctx, nx, ny, nz, glaw, x, u, w.ap, mask, st);
+    if (rc) return rc;
+    pcg_init_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, b, w.ap, mask, w.dinv, w.r, w.p1, u, w.partials, w.sc, rtol,
+                                                        max_iter);
+    GBS_LAUNCH_CHECK("pcg_init_kernel");
+    PcgScalars h;
+    rc = read_scalars(w.sc, &h, st);
+    if (rc) return rc;
+    int chunk = check_every > 0 ? check_every : 16;
+    int launched = 0;
+    while (!h.done && launched < max_iter) {
+        const int n = (launched + chunk > max_iter) ? (max_iter - launched) : chunk;
+        for (int i = 0; i < n; ++i) {
+            rc = pcg_iteration(ctx, nx, ny, nz, law, x, mask, u, w, st);
+            if (rc) return rc;
+        }
+        launched += n;
+        rc = read_scalars(w.sc, &h, st);
+        if (rc) return rc;
+        if (check_every <= 0 && chunk < 128) chunk *= 2;
+    }
+    pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc);
+    GBS_LAUNCH_CHECK("pcg_finalize_kernel");
+    rc = read_scalars(w.sc, &h, st);
+    if (rc) return rc;
+    *out = h;
+    return GBS_OK;
+}
+
+// ---- FP64 outer defect correction ---------------------------------------------------------
+struct OuterScalars {
+    double ff;      // ||D f||^2
+    double rr;      // ||D(f - K u)||^2
+    double scale;   // 1/||r|| used to form the FP32 right-hand side
+    unsigned counter;
+    int pad;
+};
+
+struct SolveWs {
+    OuterScalars *os;
+    double *r64;
+    float *b32, *d32;
+    double *partials;
+    void *pcg;
+};
+
+static size_t solve_ws_bytes_impl(int nx, int ny, int nz) {
+    const size_t nd = (size_t)n_dof_of(nx, ny, nz);
+    return al256(sizeof(OuterScalars)) + al256(nd * 8) + 2 * al256(nd * 4) + al256(3 * 4096 * 8) +
+           pcg_ws_bytes_impl(nx, ny, nz);
+}
+
+static SolveWs solve_ws(void *ws, int nx, int ny, int nz) {
+    const size_t nd = (size_t)n_dof_of(nx, ny, nz);
+    char *p = (char *)ws;
+    SolveWs w;
+    w.os = (OuterScalars *)p;
+    p += al256(sizeof(OuterScalars));
+    w.r64 = (double *)p;
+    p += al256(nd * 8);
+    w.b32 = (float *)p;
+    p += al256(nd * 4);
+    w.d32 = (float *)p;
+    p += al256(nd * 4);
+    w.partials = (double *)p;
+    p += al256(3 * 4096 * 8);
+    w.pcg = p;
+    return w;
+}
+
+// r = D f - q (q = D K D u); ||r||^2, ||D f||^2 -> os.
+__global__ void resid64_kernel(int64_t nd, const double *__restrict__ f, const double *__restrict__ q,
+                               const uint8_t *__restrict__ mask, double *r, double *partials, OuterScalars *os) {
+    double rr = 0.0, ff = 0.0;
+    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
+        const bool fx = dof_fixed(mask, d);
+        const double fd = fx ? 0.0 : f[d];
+        const double rd = fx ? 0.0 : fd - q[d];
+        r[d] = rd;
+        rr = fma(rd, rd, rr);
+        ff = fma(fd, fd, ff);
+    }
+    __shared__ double tot[3];
+    if (last_block3(rr, ff, 0.0, partials, &os->counter, tot) && threadIdx.x == 0) {
+        os->rr = tot[0];
+        os->ff = tot[1];
+        os->scale = tot[0] > 0.0 ? 1.0 / sqrt(tot[0]) : 0.0;
+    }
+}
+
+__global__ void scale_to_f32_kernel(int64_t nd, const double *__restrict__ r, const OuterScalars *os, float *b,
+                                    float *d) {
+    const double s = os->scale;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x) {
+        b[i] = (float)(r[i] * s);
+        d[i] = 0.0f;
+    }
+}
+
+__global__ void correct64_kernel(int64_t nd, const float *__restrict__ d, const OuterScalars *os,
+                                 const uint8_t *__restrict__ mask, double *u) {
+    const double s = os->scale > 0.0 ? 1.0 / os->scale : 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x)
+        u[i] = dof_fixed(mask, i) ? 0.0 : fma((double)d[i], s, u[i]);
+}
+
+static int read_outer(const OuterScalars *d, OuterScalars *h, cudaStream_t st) {
+    void *hp = thread_pinned();
+    if (!hp) return set_error(GBS_ECUDA, "no pinned staging buffer");
+    GBS_CUDA_TRY(cudaMemcpyAsync(hp, d, sizeof(OuterScalars), cudaMemcpyDeviceToHost, st));
+    GBS_CUDA_TRY(cudaStreamSynchronize(st));
+    memcpy(h, hp, sizeof(OuterScalars));
+    return GBS_OK;
+}
+
+int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x, const double *f,
+              const uint8_t *mask, double *u, const gbsimp_solve_opts *o, gbsimp_solve_stats *stats, void *ws,
+              cudaStream_t st) {
+    const int64_t nd = n_dof_of(nx, ny, nz);
+    SolveWs w = solve_ws(ws, nx, ny, nz);
+    GBS_CUDA_TRY(cudaMemsetAsync(w.os, 0, sizeof(OuterScalars), st));
+    const unsigned vb = vec_blocks(ctx, nd);
+    int total = 0, outer = 0, status = GBS_OK;
+    double relres = 0.0;
+    const int max_outer = o->max_outer > 0 ? o->max_outer : 20;
+    const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-3;
+    for (;;) {
+        int rc = apply_f64(ctx, nx, ny, nz, law, x, u, w.r64, mask, st);
+        if (rc) return rc;
+        // resid64 reads q from r64 and overwrites it in place (element-wise, same index).
+        resid64_kernel<<<vb, 256, 0, st>>>(nd, f, w.r64, mask, w.r64, w.partials, w.os);
+        GBS_LAUNCH_CHECK("resid64_kernel");
+        OuterScalars h;
+        rc = read_outer(w.os, &h, st);
+        if (rc) return rc;
+        ++outer;
+        if (!isfinite(h.rr) || !isfinite(h.ff)) {
+            status = GBS_ENONFINITE;
+            break;
+        }
+        if (h.ff == 0.0) {
+            GBS_CUDA_TRY(cudaMemsetAsync(u, 0, nd * sizeof(double), st));
+            relres = 0.0;
+            break;
+        }
+        relres = sqrt(h.rr / h.ff);
+        if (relres <= o->rtol) break;
+        if (outer > max_outer || total >= o->max_iter) {
+            status = GBS_ENOTCONV;
+            break;
+        }
+        scale_to_f32_kernel<<<vb, 256, 0, st>>>(nd, w.r64, w.os, w.b32, w.d32);
+        GBS_LAUNCH_CHECK("scale_to_f32_kernel");
+        // Inner tolerance: enough to reach rtol from here, but not below what FP32 resolves.
+        double itol = o->rtol / relres;
+        if (itol < inner) itol = inner;
+        PcgScalars ps;
+        rc = pcg_run(ctx, nx, ny, nz, law, x, w.b32, mask, w.d32, itol, o->max_iter - total, o->check_every, w.pcg,
+                     &ps, st);
+        if (rc) return rc;
+        total += ps.iter;
+        if (ps.status == GBS_EBREAKDOWN || ps.status == GBS_ENONFINITE) {
+            status = ps.status;
+            if (ps.iter == 0) break;
+        }
+        correct64_kernel<<<vb, 256, 0, st>>>(nd, w.d32, w.os, mask, u);
+        GBS_LAUNCH_CHECK("correct64_kernel");
+        if (status != GBS_OK) break;
+    }
+    if (stats) {
+        stats->status = status;
+        stats->iterations = total;
+        stats->outer = outer;
+        stats->relres = relres;
+    }
+    return GBS_OK;
+}
+
+// ---- CSR Jacobi-PCG (pcg_solve_cuda contract) -------------------------------------------------
+struct CsrScalars {
+    double rz, rr, bnorm, alpha, beta, pap;
+    int iter, done, status, max_iter;
+    double tol;
+    unsigned counter;
+    int pad;
+};
+
+// Warp per row.
+__global__ void csr_spmv_kernel(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                                const float *__restrict__ v, const float *__restrict__ p, float *y) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = warp; row < n; row += nw) {
+        const int32_t b = rp[row], e = rp[row + 1];
+        float s = 0.0f;
+        for (int32_t k = b + lane; k < e; k += 32) {
+            const int32_t c = ci[k];
+            if (c >= 0 && c < n) s = fmaf(v[k], p[c], s);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) y[row] = s;
+    }
+}
+
+__global__ void zero_list_kernel(int64_t m, const int32_t *__restrict__ idx, int64_t n, float *v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t d = idx[i];
+        if (d >= 0 && d < n) v[d] = 0.0f;
+    }
+}
+
+__global__ void csr_init_kernel(int64_t n, const float *__restrict__ b, const float *__restrict__ q, float *r,
+                                double *partials, CsrScalars *sc) {
+    double bb = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        r[i] = b[i] - q[i];
+        bb += (double)b[i] * (double)b[i];
+    }
+    __shared__ double tot[3];
+    if (last_block3(bb, 0.0, 0.0, partials, &sc->counter, tot) && threadIdx.x == 0) sc->bnorm = sqrt(tot[0]);
+}
+
+__global__ void csr_z_kernel(int64_t n, const float *__restrict__ r, const float *__restrict__ diag, float *z,
+                             float *p, int set_p, double *partials, CsrScalars *sc) {
+    if (!set_p && sc->done) return;
+    double rz = 0.0;
+    const float beta = set_p ? 0.0f : (float)sc->beta;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float zi = r[i] / diag[i];
+        z[i] = zi;
+        rz += (double)r[i] * (double)zi;
+    }
+    __shared__ double tot[3];
+    if (last_block3(rz, 0.0, 0.0, partials, &sc->counter, tot) && threadIdx.x == 0) {
+        if (set_p) {
+            sc->rz = tot[0];
+        } else {
+            sc->beta = tot[0] / sc->rz;
+            sc->rz = tot[0];
+        }
+    }
+    (void)p;
+    (void)beta;
+}
+
+__global__ void csr_p_kernel(int64_t n, const float *__restrict__ z, float *p, int first, const CsrScalars *sc) {
+    if (!first && sc->done) return;
+    const float beta = first ? 0.0f : (float)sc->beta;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = first ? z[i] : fmaf(beta, p[i], z[i]);
+}
+
+__global__ void csr_pap_kernel(int64_t n, const float *__restrict__ p, const float *__restrict__ ap, double *partials,
+                               CsrScalars *sc) {
+    if (sc->done) return;
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += (double)p[i] * (double)ap[i];
+    __shared__ double tot[3];
+    if (last_block3(s, 0.0, 0.0, partials, &sc->counter, tot) && threadIdx.x == 0) {
+        sc->pap = tot[0];
+        if (fabs(tot[0]) < 1e-30 || !isfinite(tot[0])) {  // simp_pcg_cuda.cu:102
+            sc->done = 1;
+            sc->status = isfinite(tot[0]) ? GBS_EBREAKDOWN : GBS_ENONFINITE;
+        } else {
+            sc->alpha = sc->rz / tot[0];
+        }
+    }
+}
+
+__global__ void csr_xr_kernel(int64_t n, const float *__restrict__ p, const float *__restrict__ ap, float *x, float *r,
+                              const int32_t *__restrict__ fixed, int64_t n_fixed, CsrScalars *sc) {
+    if (sc->done) return;
+    const float a = (float)sc->alpha;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] = fmaf(a, p[i], x[i]);
+        r[i] = fmaf(-a, ap[i], r[i]);
+    }
+    (void)fixed;
+    (void)n_fixed;
+}
+
+__global__ void csr_check_kernel(int64_t n, const float *__restrict__ r, double *partials, CsrScalars *sc) {
+    if (sc->done) return;
+    double s = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += (double)r[i] * (double)r[i];
+    __shared__ double tot[3];
+    if (last_block3(s, 0.0, 0.0, partials, &sc->counter, tot) && threadIdx.x == 0) {
+        sc->rr = tot[0];
+        sc->iter += 1;
+        if (!isfinite(tot[0])) {
+            sc->done = 1;
+            sc->status = GBS_ENONFINITE;
+        } else if (sqrt(tot[0]) < sc->tol * sc->bnorm) {
+            sc->done = 1;
+        } else if (sc->iter >= sc->max_iter) {
+            sc->done = 1;
+            sc->status = GBS_ENOTCONV;
+        }
+    }
+}
+
+struct CsrWs {
+    CsrScalars *sc;
+    float *r, *z, *p, *ap;
+    double *partials;
+};
+
+static size_t csr_ws_bytes_impl(int64_t n) { return al256(sizeof(CsrScalars)) + 4 * al256((size_t)n * 4) + al256(3 * 4096 * 8); }
+
+static CsrWs csr_ws(void *ws, int64_t n) {
+    char *p = (char *)ws;
+    CsrWs w;
+    w.sc = (CsrScalars *)p;
+    p += al256(sizeof(CsrScalars));
+    float **v[4] = {&w.r, &w.z, &w.p, &w.ap};
+    for (int i = 0; i < 4; ++i) {
+        *v[i] = (float *)p;
+        p += al256((size_t)n * 4);
+    }
+    w.partials = (double *)p;
+    return w;
+}
+
+}  // namespace gbs
+
+using namespace gbs;
+
+extern "C" size_t gbsimp_pcg_ws_bytes(int nx, int ny, int nz) { return pcg_ws_bytes_impl(nx, ny, nz); }
+
+extern "C" size_t gbsimp_solve_ws_bytes(int nx, int ny, int nz) { return solve_ws_bytes_impl(nx, ny, nz); }
+
+extern "C" size_t gbsimp_pcg_csr_ws_bytes(int64_t n) { return csr_ws_bytes_impl(n); }
+
+static bool grid_ok(int nx, int ny, int nz) {
+    return nx > 0 && ny > 0 && nz > 0 && (int64_t)(nx + 1) * (ny + 1) * (nz + 1) < (1LL << 31) / 3;
+}
+
+extern "C" int gbsimp_pcg_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
+                              const float *b, const uint8_t *node_mask, float *u, const gbsimp_solve_opts *opts,
+                              gbsimp_solve_stats *stats, void *ws, size_t ws_bytes, void *stream) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (!ctx || !law || !x || !b || !u || !opts || !ws || !grid_ok(nx, ny, nz))
+        return set_error(GBS_EINVAL, "gbsimp_pcg_f32: bad arguments");
+    if (ws_bytes < pcg_ws_bytes_impl(nx, ny, nz)) return set_error(GBS_EINVAL, "gbsimp_pcg_f32: workspace too small");
+    PcgScalars h;
+    int rc = pcg_run(ctx, nx, ny, nz, law, x, b, node_mask, u, opts->rtol, opts->max_iter, opts->check_every, ws, &h,
+                     (cudaStream_t)stream);
+    if (rc) return rc;
+    if (stats) {
+        stats->status = h.status;
+        stats->iterations = h.iter;
+        stats->outer = 0;
+        stats->relres = h.bnorm > 0.0 ? sqrt(h.rr) / h.bnorm : 0.0;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return GBS_OK;
+}
+
+extern "C" int gbsimp_solve(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
+                            const double *f, const uint8_t *node_mask, double *u, const gbsimp_solve_opts *opts,
+                            gbsimp_solve_stats *stats, void *ws, size_t ws_bytes, void *stream) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (!ctx || !law || !x || !f || !u || !opts || !ws || !grid_ok(nx, ny, nz))
+        return set_error(GBS_EINVAL, "gbsimp_solve: bad arguments");
+    if (ws_bytes < solve_ws_bytes_impl(nx, ny, nz)) return set_error(GBS_EINVAL, "gbsimp_solve: workspace too small");
+    gbsimp_solve_stats s{};
+    int rc = solve_run(ctx, nx, ny, nz, law, x, f, node_mask, u, opts, &s, ws, (cudaStream_t)stream);
+    if (rc) return rc;
+    s.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (stats) *stats = s;
+    return GBS_OK;
+}
+
+extern "C" int gbsimp_pcg_csr_f32(gbsimp_ctx *ctx, int64_t n, const int32_t *row_ptr, const int32_t *col_idx,
+                                  const float *values, const float *diagonal, const float *b, float *x,
+                                  const int32_t *fixed, int64_t n_fixed, const gbsimp_solve_opts *opts,
+                                  gbsimp_solve_stats *stats, void *ws, size_t ws_bytes, void *stream) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (!ctx || n <= 0 || !row_ptr || !col_idx || !values || !diagonal || !b || !x || !opts || !ws ||
+        (n_fixed > 0 && !fixed) || n >= (1LL << 31))
+        return set_error(GBS_EINVAL, "gbsimp_pcg_csr_f32: bad arguments");
+    if (ws_bytes < csr_ws_bytes_impl(n)) return set_error(GBS_EINVAL, "gbsimp_pcg_csr_f32: workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    CsrWs w = csr_ws(ws, n);
+    const unsigned vb = vec_blocks(ctx, n);
+    unsigned sb = (unsigned)((n * 32 + 255) / 256);
+    if (sb > 8u * (unsigned)ctx->num_sms) sb = 8u * (unsigned)ctx->num_sms;
+    if (sb < 1) sb = 1;
+    const unsigned fb = n_fixed > 0 ? vec_blocks(ctx, n_fixed) : 1;
+    CsrScalars init{};
+    init.tol = opts->rtol;
+    init.max_iter = opts->max_iter;
+    void *hp = thread_pinned();
+    if (!hp) return set_error(GBS_ECUDA, "no pinned staging buffer");
+    memcpy(hp, &init, sizeof init);
+    GBS_CUDA_TRY(cudaMemcpyAsync(w.sc, hp, sizeof init, cudaMemcpyHostToDevice, st));
+    // r = b - A x0; r[fixed] = 0; z = r/diag; p = z; rz = r.z
+    csr_spmv_kernel<<<sb, 256, 0, st>>>(n, row_ptr, col_idx, values, x, w.ap);
+    csr_init_kernel<<<vb, 256, 0, st>>>(n, b, w.ap, w.r, w.partials, w.sc);
+    if (n_fixed > 0) zero_list_kernel<<<fb, 256, 0, st>>>(n_fixed, fixed, n, w.r);
+    csr_z_kernel<<<vb, 256, 0, st>>>(n, w.r, diagonal, w.z, w.p, 1, w.partials, w.sc);
+    csr_p_kernel<<<vb, 256, 0, st>>>(n, w.z, w.p, 1, w.sc);
+    GBS_LAUNCH_CHECK("csr setup");
+    const int chunk = opts->check_every > 0 ? opts->check_every : 32;
+    CsrScalars h{};
+    int launched = 0;
+    while (launched < opts->max_iter) {
+        const int m = launched + chunk > opts->max_iter ? opts->max_iter - launched : chunk;
+        for (int i = 0; i < m; ++i) {
+            csr_spmv_kernel<<<sb, 256, 0, st>>>(n, row_ptr, col_idx, values, w.p, w.ap);
+            if (n_fixed > 0) zero_list_kernel<<<fb, 256, 0, st>>>(n_fixed, fixed, n, w.ap);
+            csr_pap_kernel<<<vb, 256, 0, st>>>(n, w.p, w.ap, w.partials, w.sc);
+            csr_xr_kernel<<<vb, 256, 0, st>>>(n, w.p, w.ap, x, w.r, fixed, n_fixed, w.sc);
+            if (n_fixed > 0) zero_list_kernel<<<fb, 256, 0, st>>>(n_fixed, fixed, n, w.r);
+            csr_check_kernel<<<vb, 256, 0, st>>>(n, w.r, w.partials, w.sc);
+            csr_z_kernel<<<vb, 256, 0, st>>>(n, w.r, diagonal, w.z, w.p, 0, w.partials, w.sc);
+            csr_p_kernel<<<vb, 256, 0, st>>>(n, w.z, w.p, 0, w.sc);
+        }
+        GBS_LAUNCH_CHECK("csr iteration");
+        launched += m;
+        GBS_CUDA_TRY(cudaMemcpyAsync(hp, w.sc, sizeof h, cudaMemcpyDeviceToHost, st));
+        GBS_CUDA_TRY(cudaStreamSynchronize(st));
+        memcpy(&h, hp, sizeof h);
+        if (h.done) break;
+    }
+    if (stats) {
+        stats->status = h.done ? h.status : GBS_ENOTCONV;
+        stats->iterations = h.iter;
+        stats->outer = 0;
+        stats->relres = h.bnorm > 0.0 ? sqrt(h.rr) / h.bnorm : 0.0;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return GBS_OK;
+}

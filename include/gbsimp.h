@@ -1,0 +1,198 @@
+/*
+ * gbsimp.h -- C ABI of the GB300 (sm_103a) SIMP / voxel-FEM hot path.
+ *
+ * One shared library (genpipeline_gb300/libgbsimp.so). Plain C types only: every array
+ * argument is a raw device pointer owned by the caller, every size is an explicit
+ * integer, every call is ordered on the caller's CUDA stream (passed as void*) and none
+ * of them synchronises the device unless its comment says it returns host-visible
+ * results. Scratch memory is caller-owned too: each call that needs scratch takes
+ * (ws, ws_bytes) and a *_ws_bytes() query says how much.
+ *
+ * Layout (identical to the reference genpipeline/topology/simp_solver.py:251-282):
+ *   element e = i*ny*nz + j*nz + k   (0 <= i < nx, ...)
+ *   node    n = i*(ny+1)*(nz+1) + j*(nz+1) + k
+ *   DOF       = 3n + c  (c = x, y, z)
+ *   element-local node a in the order (0,0,0),(1,0,0),(1,1,0),(0,1,0),(0,0,1),(1,0,1),
+ *   (1,1,1),(0,1,1); element-local DOF 3a + c; Ke is row-major 24x24.
+ * Dirichlet masks are one byte per node: bit c set = DOF 3n+c is fixed (held at 0).
+ *
+ * Return values: GBS_OK or one of the GBS_E* codes; gbsimp_last_error() gives the
+ * message of the last failure on the calling thread.
+ */
+#ifndef GBSIMP_H
+#define GBSIMP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBSIMP_ABI_VERSION 1
+
+enum {
+    GBS_OK = 0,
+    GBS_EINVAL = 1,      /* bad argument (sizes, null pointers, too-small workspace) */
+    GBS_ENOMEM = 2,      /* host allocation failed */
+    GBS_ENOTCONV = 3,    /* iteration cap reached; the best iterate is still written */
+    GBS_EBREAKDOWN = 4,  /* p^T K p <= 0 in CG (operator not SPD on the free DOFs) */
+    GBS_ETIMEOUT = 5,    /* a bounded device-side wait expired */
+    GBS_ECUDA = 6,       /* a CUDA runtime call failed */
+    GBS_ENONFINITE = 7   /* NaN/Inf met in a residual or a reduction */
+};
+
+/* Stiffness law of one element: kind 0 ("ref", simp_solver.py:182-185)
+ *   E = e0 * max(x, xmin)^penal,            dE/dx = e0 * penal * max(x, xmin)^(penal-1)
+ * kind 1 ("modified", the SIMP law of simp_sensitivity_ptx.cu:20-26)
+ *   E = emin + x^penal * (e0 - emin),       dE/dx = penal * x^(penal-1) * (e0 - emin)   */
+typedef struct gbsimp_law {
+    int32_t kind;
+    int32_t reserved;
+    double penal, e0, emin, xmin;
+} gbsimp_law;
+
+/* OC bisection parameters (simp_solver.py:225-249 = CPU variant:
+ *   move 0.2, l1 0, l2 1e9, max_bisect 50, tol 1e-4, tol_eps 1e-12, sqrt_floor 1e-12;
+ * simp_solver_gpu.py:801-841 = GPU variant: l2 < 0 requests l2 = 2*max(max(-dc), 1),
+ *   max_bisect 30, tol 1e-5, tol_eps 1e-15, sqrt_floor 1e-15). */
+typedef struct gbsimp_oc_params {
+    double move, l1, l2, tol, tol_eps, sqrt_floor, volfrac;
+    int32_t max_bisect;
+    int32_t reserved;
+} gbsimp_oc_params;
+
+/* Options and results of the linear solves. */
+typedef struct gbsimp_solve_opts {
+    double rtol;          /* stop when ||D(f - K u)|| <= rtol * ||D f|| (FP64 residual) */
+    double inner_rtol;    /* FP32 PCG reduction per outer correction (gbsimp_solve only) */
+    int32_t max_iter;     /* cap on the total FP32 PCG iterations */
+    int32_t max_outer;    /* cap on FP64 defect corrections (gbsimp_solve only) */
+    int32_t check_every;  /* iterations between host-side convergence checks (0 = auto) */
+    int32_t fused;        /* 1 = persistent fused PCG kernel, 0 = one launch per step */
+} gbsimp_solve_opts;
+
+typedef struct gbsimp_solve_stats {
+    int32_t status;       /* GBS_OK, GBS_ENOTCONV, GBS_EBREAKDOWN, GBS_ENONFINITE, GBS_ETIMEOUT */
+    int32_t iterations;   /* FP32 PCG iterations (all outer corrections together) */
+    int32_t outer;        /* FP64 residual evaluations */
+    int32_t reserved;
+    double relres;        /* last ||D(f - K u)|| / ||D f|| */
+    double seconds;       /* host wall time of the call */
+} gbsimp_solve_stats;
+
+typedef struct gbsimp_ctx gbsimp_ctx;
+
+/* ---- context ---------------------------------------------------------------------- */
+int gbsimp_abi_version(void);
+const char *gbsimp_last_error(void);
+/* Creates a context bound to the current CUDA device, holding the quadrature element
+ * stiffness of (nu = 0.3, E = 1). No device memory is allocated. */
+int gbsimp_create(gbsimp_ctx **out);
+int gbsimp_destroy(gbsimp_ctx *ctx);
+/* Unit-cube trilinear hexahedron by 2x2x2 Gauss quadrature of B^T D B (host, FP64). The
+ * reference's own table (simp_solver.py:284-1543, reused by simp_solver_gpu.py:932-936)
+ * is not symmetric positive semi-definite; this is the SPD matrix of the same element. */
+int gbsimp_ke_quadrature(double nu, double e0, double *ke576);
+/* Replaces the context's element stiffness (host pointer, 576 doubles, row-major). */
+int gbsimp_set_ke(gbsimp_ctx *ctx, const double *ke576);
+int gbsimp_get_ke(const gbsimp_ctx *ctx, double *ke576);
+
+/* ---- element stiffness apply ------------------------------------------------------- */
+/* y = D K(x) D p with K(x) = sum_e E(x_e) P_e^T Ke P_e; D zeroes the DOFs flagged in
+ * node_mask (nullable: no masking). Replaces the COO assembly + SpMV of
+ * simp_solver.py:200-205 / simp_solver_gpu.py:313-326 and fused_spmv_kernel
+ * (cuda_kernels/simp_sensitivity_ptx.cu:301-373). Owner-computes, no atomics. */
+int gbsimp_apply_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
+                     const float *x, const float *p, float *y, const uint8_t *node_mask,
+                     void *stream);
+int gbsimp_apply_f64(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
+                     const float *x, const double *p, double *y, const uint8_t *node_mask,
+                     void *stream);
+/* Same operator over an arbitrary element->DOF table edof[n_elem][24] (int32 or int64 per
+ * edof_is_int64), the contract of cuda_kernels.fused_spmv (cuda_kernels/__init__.py:329-368).
+ * y (n_dof floats) is overwritten; contributions are summed with atomics. */
+int gbsimp_apply_edof_f32(gbsimp_ctx *ctx, int64_t n_elem, int64_t n_dof, const void *edof,
+                          int edof_is_int64, const gbsimp_law *law, const float *x,
+                          const float *p, float *y, void *stream);
+
+/* ---- element energy / sensitivity -------------------------------------------------- */
+/* ce_e = u_e^T Ke u_e, dc_e = -dE/dx(x_e) * ce_e (simp_solver.py:215-218,
+ * simp_sensitivity_kernel in cuda_kernels/simp_sensitivity_ptx.cu:163-270), computed in
+ * FP64 from the FP64 displacement. dc and ce are nullable FP32 outputs; energy_out
+ * (nullable, device double) receives sum_e E_e ce_e = u^T K u. */
+size_t gbsimp_sensitivity_ws_bytes(int nx, int ny, int nz);
+int gbsimp_sensitivity(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
+                       const float *x, const double *u, float *dc, float *ce,
+                       double *energy_out, void *ws, size_t ws_bytes, void *stream);
+/* Arbitrary edof table and FP32 u (cuda_kernels.simp_sensitivity, __init__.py:286-326). */
+int gbsimp_sensitivity_edof_f32(gbsimp_ctx *ctx, int64_t n_elem, int64_t n_dof,
+                                const void *edof, int edof_is_int64, const gbsimp_law *law,
+                                const float *x, const float *u, float *dc, void *stream);
+
+/* ---- density filter ---------------------------------------------------------------- */
+/* H[e1,e2] = rmin - dist(e1,e2) for dist <= rmin (clipped at the grid boundary),
+ * Hs = row sums (simp_solver.py:1545-1567). transpose 0: out = H in / Hs (simp_solver.py:237);
+ * transpose 1: out = H^T (in / Hs) (simp_solver.py:221-223). rmin <= 6. hs: nullable
+ * precomputed row sums (from gbsimp_filter_hs), else computed on the fly. */
+int gbsimp_filter_hs(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, float *hs,
+                     void *stream);
+int gbsimp_filter(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const float *hs,
+                  const float *in, float *out, int transpose, void *stream);
+
+/* ---- OC update --------------------------------------------------------------------- */
+/* Bisection on the Lagrange multiplier (simp_solver.py:225-249; parameters above).
+ * The volume of each trial is sum_e w_e xnew_e + n_preserved with the precomputed weights
+ * w = H^T(m / Hs), m_e = 0 on preserved elements else 1 (same value as mean(H xnew / Hs)
+ * with the preserved entries set to 1). Bisection runs on the device (no host sync).
+ * Outputs: xnew, xphys (= H xnew / Hs, preserved -> 1), and in the workspace the final
+ * multiplier and step count, copied to host by gbsimp_oc_result(). preserved nullable. */
+size_t gbsimp_oc_ws_bytes(int nx, int ny, int nz);
+int gbsimp_oc_prepare(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin,
+                      const uint8_t *preserved, void *ws, size_t ws_bytes, void *stream);
+int gbsimp_oc(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin,
+              const gbsimp_oc_params *prm, const float *x, const float *dc,
+              const uint8_t *preserved, float *xnew, float *xphys, void *ws, size_t ws_bytes,
+              void *stream);
+/* Synchronises the stream; returns lambda and bisection steps of the last gbsimp_oc. */
+int gbsimp_oc_result(gbsimp_ctx *ctx, const void *ws, double *lambda_out, int *steps_out,
+                     void *stream);
+
+/* ---- linear solves ----------------------------------------------------------------- */
+/* FP32 Jacobi-PCG on the free DOFs (simp_solver_gpu.py:328-379, _solve :571-705):
+ * u holds x0 on entry (fixed DOFs are zeroed), the solution on exit. The stop test is
+ * ||r|| < rtol ||D b||, checked on the device every iteration; the host reads the
+ * status every opts->check_every iterations (the call synchronises the stream). */
+size_t gbsimp_pcg_ws_bytes(int nx, int ny, int nz);
+int gbsimp_pcg_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
+                   const float *x, const float *b, const uint8_t *node_mask, float *u,
+                   const gbsimp_solve_opts *opts, gbsimp_solve_stats *stats, void *ws,
+                   size_t ws_bytes, void *stream);
+/* FP32 PCG inner solves with FP64 outer defect correction: r = D(f - K u) in FP64, FP32
+ * PCG on K d = r to inner_rtol, u += d, until ||r|| <= rtol ||D f||. u (FP64) holds the
+ * warm start on entry. Synchronises the stream. */
+size_t gbsimp_solve_ws_bytes(int nx, int ny, int nz);
+int gbsimp_solve(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
+                 const float *x, const double *f, const uint8_t *node_mask, double *u,
+                 const gbsimp_solve_opts *opts, gbsimp_solve_stats *stats, void *ws,
+                 size_t ws_bytes, void *stream);
+/* Jacobi-PCG on a CSR matrix (int32 row_ptr/col_idx, FP32 values, FP32 diagonal), the
+ * contract of cuda_kernels.pcg_solve_cuda (cuda_kernels/__init__.py:443-473,
+ * simp_pcg_cuda.cu:66-124): x holds x0 on entry; fixed is a list of n_fixed DOF indices
+ * whose residual entries are zeroed. Synchronises the stream. */
+size_t gbsimp_pcg_csr_ws_bytes(int64_t n);
+int gbsimp_pcg_csr_f32(gbsimp_ctx *ctx, int64_t n, const int32_t *row_ptr,
+                       const int32_t *col_idx, const float *values, const float *diagonal,
+                       const float *b, float *x, const int32_t *fixed, int64_t n_fixed,
+                       const gbsimp_solve_opts *opts, gbsimp_solve_stats *stats, void *ws,
+                       size_t ws_bytes, void *stream);
+
+/* ---- reductions used by the host loops -------------------------------------------- */
+/* out (device double) = sum_i a_i * b_i over n FP64 entries, fixed block order. */
+int gbsimp_dot_f64(gbsimp_ctx *ctx, int64_t n, const double *a, const double *b,
+                   double *out, void *ws, size_t ws_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBSIMP_H */
