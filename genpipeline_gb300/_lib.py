@@ -51,17 +51,20 @@ class OcParams(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("inner_rtol", C.c_double), ("max_iter", C.c_int32),
-                ("max_outer", C.c_int32), ("check_every", C.c_int32), ("fused", C.c_int32)]
+                ("max_outer", C.c_int32), ("check_every", C.c_int32), ("fused", C.c_int32),
+                ("profile", C.c_int32), ("reserved", C.c_int32)]
 
 
 class SolveStats(C.Structure):
     _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("outer", C.c_int32),
-                ("reserved", C.c_int32), ("relres", C.c_double), ("seconds", C.c_double)]
+                ("reserved", C.c_int32), ("relres", C.c_double), ("seconds", C.c_double),
+                ("apply_seconds", C.c_double), ("apply_launches", C.c_int32), ("reserved2", C.c_int32)]
 
     def as_dict(self):
         return {"status": int(self.status), "status_name": STATUS_NAMES.get(int(self.status), "?"),
                 "iterations": int(self.iterations), "outer": int(self.outer),
-                "relres": float(self.relres), "seconds": float(self.seconds)}
+                "relres": float(self.relres), "seconds": float(self.seconds),
+                "apply_seconds": float(self.apply_seconds), "apply_launches": int(self.apply_launches)}
 
 
 _P = C.c_void_p
@@ -73,6 +76,7 @@ _SZ = C.c_size_t
 # name -> (restype, argtypes); the list mirrors include/gbsimp.h one to one.
 SIGNATURES = {
     "gbsimp_abi_version": (_I, []),
+    "gbsimp_launch_count": (C.c_uint64, []),
     "gbsimp_last_error": (C.c_char_p, []),
     "gbsimp_create": (_I, [C.POINTER(_P)]),
     "gbsimp_destroy": (_I, [_P]),

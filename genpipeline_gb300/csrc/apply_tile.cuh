@@ -86,8 +86,18 @@ __global__ void __launch_bounds__(TX *TY *TZ)
         pnew = (it & 1) ? pa.pbuf1 : pa.pbuf0;
     }
 
-    // ---- stage p (halo) --------------------------------------------------------------
-    for (int t = tid; t < HX * HY * HZ * 3; t += NT) {
+    // ---- stage p (halo) and E(x): all global loads of a thread are issued before any
+    // shared-memory store (unrolled, compile-time trip counts) so their latencies overlap.
+    constexpr int NPV = HX * HY * HZ * 3;
+    constexpr int IPV = (NPV + NT - 1) / NT;
+    constexpr int NEV = EX * EY * EZ;
+    constexpr int IEV = (NEV + NT - 1) / NT;
+    T pv[IPV];
+    float xv[IEV];
+    bool xok[IEV];
+#pragma unroll
+    for (int q = 0; q < IPV; ++q) {
+        const int t = tid + q * NT;
         const int c = t % 3;
         const int rest = t / 3;
         const int hz = rest % HZ;
@@ -95,27 +105,36 @@ __global__ void __launch_bounds__(TX *TY *TZ)
         const int hx = rest / (HZ * HY);
         const int gx = x0 - 1 + hx, gy = y0 - 1 + hy, gz = z0 - 1 + hz;
         T v = (T)0;
-        if (gx >= 0 && gx <= nx && gy >= 0 && gy <= ny && gz >= 0 && gz <= nz) {
+        if (t < NPV && gx >= 0 && gx <= nx && gy >= 0 && gy <= ny && gz >= 0 && gz <= nz) {
             const int64_t d = 3 * (((int64_t)gx * NY + gy) * NZ + gz) + c;
             if (MODE == MODE_PLAIN) {
                 v = A.p[d];
                 if (A.mask && ((A.mask[d / 3] >> c) & 1)) v = (T)0;
             } else {
-                v = (T)(pa.r[d] * pa.dinv[d] + (float)beta * pold[d]);
+                v = (T)fmaf((float)beta, pold[d], pa.r[d] * pa.dinv[d]);
             }
         }
-        sp[t] = v;
+        pv[q] = v;
     }
-    // ---- stage E(x) of the touching elements ------------------------------------------
-    for (int t = tid; t < EX * EY * EZ; t += NT) {
+#pragma unroll
+    for (int q = 0; q < IEV; ++q) {
+        const int t = tid + q * NT;
         const int ez = t % EZ;
         const int ey = (t / EZ) % EY;
         const int ex = t / (EZ * EY);
         const int gx = x0 - 1 + ex, gy = y0 - 1 + ey, gz = z0 - 1 + ez;
-        T v = (T)0;
-        if (gx >= 0 && gx < nx && gy >= 0 && gy < ny && gz >= 0 && gz < nz)
-            v = modulus(law, (T)A.x[((int64_t)gx * ny + gy) * nz + gz]);
-        se[t] = v;
+        xok[q] = t < NEV && gx >= 0 && gx < nx && gy >= 0 && gy < ny && gz >= 0 && gz < nz;
+        xv[q] = xok[q] ? A.x[((int64_t)gx * ny + gy) * nz + gz] : 0.0f;
+    }
+#pragma unroll
+    for (int q = 0; q < IPV; ++q) {
+        const int t = tid + q * NT;
+        if (t < NPV) sp[t] = pv[q];
+    }
+#pragma unroll
+    for (int q = 0; q < IEV; ++q) {
+        const int t = tid + q * NT;
+        if (t < NEV) se[t] = xok[q] ? modulus(law, (T)xv[q]) : (T)0;  // no element: E = 0
     }
     __syncthreads();
 
@@ -214,7 +233,7 @@ __global__ void __launch_bounds__(TX *TY *TZ)
 
 // Tile shapes (node bricks) per precision.
 struct TileF {
-    static constexpr int X = 2, Y = 4, Z = 32;
+    static constexpr int X = 4, Y = 4, Z = 16;
 };
 struct TileD {
     static constexpr int X = 2, Y = 2, Z = 32;

@@ -5,11 +5,16 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
+
 #include "internal.h"
 
 namespace gbs {
 
 static thread_local char g_err[512] = "";
+static std::atomic<unsigned long long> g_launches{0};
+
+void count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 
 int set_error(int code, const char *fmt, ...) {
     va_list ap;
@@ -112,6 +117,8 @@ using namespace gbs;
 extern "C" int gbsimp_abi_version(void) { return GBSIMP_ABI_VERSION; }
 
 extern "C" const char *gbsimp_last_error(void) { return g_err; }
+
+extern "C" uint64_t gbsimp_launch_count(void) { return (uint64_t)g_launches.load(); }
 
 extern "C" int gbsimp_ke_quadrature(double nu, double e0, double *ke576) {
     if (!ke576 || !(nu > -1.0 && nu < 0.5) || !(e0 > 0.0))

@@ -103,10 +103,12 @@ __device__ __forceinline__ float warp_max(float v) {
     return v;
 }
 
-// Sums v over the block; the result is valid in thread 0. scratch: >= 32 doubles.
+// Sums v over the block (1-D, 2-D or 3-D; the thread count must be a multiple of 32); the
+// result is valid in the thread with linear id 0. scratch: >= 32 doubles.
 __device__ __forceinline__ double block_sum(double v, double *scratch) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nw = (blockDim.x + 31) >> 5;
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int lane = tid & 31, warp = tid >> 5;
+    const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
     v = warp_sum(v);
     __syncthreads();
     if (lane == 0) scratch[warp] = v;
@@ -136,6 +138,7 @@ struct gbsimp_ctx {
 namespace gbs {
 int set_error(int code, const char *fmt, ...);
 int cuda_error(cudaError_t e, const char *what);
+void count_launches(int n);
 }  // namespace gbs
 
 #define GBS_CUDA_TRY(call)                                           \
@@ -146,6 +149,7 @@ int cuda_error(cudaError_t e, const char *what);
 
 #define GBS_LAUNCH_CHECK(what)                                       \
     do {                                                             \
+        gbs::count_launches(1);                                      \
         cudaError_t _e = cudaGetLastError();                         \
         if (_e != cudaSuccess) return gbs::cuda_error(_e, what);     \
     } while (0)

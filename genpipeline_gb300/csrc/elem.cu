@@ -332,9 +332,8 @@ __global__ void __launch_bounds__(256) oc_step_kernel(int64_t n, const OcParams 
     const float inv_l = (float)(1.0 / lmid);
     double v = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-        const bool pr = pres && pres[e];
-        if (pr) continue;
-        v += (double)w[e] * (double)oc_trial(x[e], dc[e], inv_l, P, false);
+        // Preserved elements hold xnew = 1 and still feed their neighbours' filtered density.
+        v += (double)w[e] * (double)oc_trial(x[e], dc[e], inv_l, P, pres && pres[e]);
     }
     const double vv[1] = {v};
     if (last_block_reduce<1>(vv, partials, &sc->counter, tot, sred) && threadIdx.x == 0) {

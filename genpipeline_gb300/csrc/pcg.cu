@@ -12,6 +12,7 @@
 #include <string.h>
 
 #include <chrono>
+#include <vector>
 
 #include "apply_tile.cuh"
 #include "internal.h"
@@ -209,7 +210,7 @@ static int read_scalars(const PcgScalars *d, PcgScalars *h, cudaStream_t st) {
 
 // Launches one K1+K2 iteration.
 static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
-                         const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st) {
+                         const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st, cudaEvent_t after_k1) {
     TileArgs<float> A{nx, ny, nz, x, nullptr, w.ap, mask};
     PcgArgs pa{w.r, w.dinv, w.p0, w.p1, u, w.partials, w.sc};
     const dim3 g = tile_grid<TileF>(nx, ny, nz), b = tile_block<TileF>();
@@ -218,6 +219,7 @@ static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const La
     else
         apply_tile_kernel<float, KeF, TileF::X, TileF::Y, TileF::Z, false, MODE_PCG><<<g, b, 0, st>>>(A, law, ctx->kef, pa);
     GBS_LAUNCH_CHECK("apply_tile_kernel<PCG>");
+    if (after_k1) GBS_CUDA_TRY(cudaEventRecord(after_k1, st));
     const int64_t nd = n_dof_of(nx, ny, nz);
     pcg_update_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.ap, w.dinv, w.r, w.partials, w.sc);
     GBS_LAUNCH_CHECK("pcg_update_kernel");
@@ -225,9 +227,16 @@ static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const La
 }
 
 // FP32 PCG. u: x0 in, solution out. Returns GBS_OK and fills *out (status inside).
+// Optional profiling (prof != nullptr): CUDA events around every K1 launch; only the
+// launches of iterations that actually ran (the device counter advanced) are summed.
+struct ApplyProfile {
+    double seconds = 0.0;
+    int launches = 0;
+};
+
 int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x, const float *b,
             const uint8_t *mask, float *u, double rtol, int max_iter, int check_every, void *ws, PcgScalars *out,
-            cudaStream_t st) {
+            cudaStream_t st, ApplyProfile *prof = nullptr) {
     const int64_t nd = n_dof_of(nx, ny, nz);
     PcgWs w = pcg_ws(ws, nx, ny, nz);
     const Law<float> law = make_law<float>(*glaw);
@@ -243,18 +252,37 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
     rc = read_scalars(w.sc, &h, st);
     if (rc) return rc;
     int chunk = check_every > 0 ? check_every : 16;
+    const int max_chunk = check_every > 0 ? check_every : 128;
+    std::vector<cudaEvent_t> ev;
+    if (prof) {
+        ev.resize(2 * (size_t)max_chunk);
+        for (auto &e : ev) GBS_CUDA_TRY(cudaEventCreate(&e));
+    }
     int launched = 0;
     while (!h.done && launched < max_iter) {
         const int n = (launched + chunk > max_iter) ? (max_iter - launched) : chunk;
+        const int it0 = h.iter;
         for (int i = 0; i < n; ++i) {
-            rc = pcg_iteration(ctx, nx, ny, nz, law, x, mask, u, w, st);
+            if (prof) GBS_CUDA_TRY(cudaEventRecord(ev[2 * i], st));
+            rc = pcg_iteration(ctx, nx, ny, nz, law, x, mask, u, w, st, prof ? ev[2 * i + 1] : nullptr);
             if (rc) return rc;
         }
         launched += n;
         rc = read_scalars(w.sc, &h, st);
         if (rc) return rc;
-        if (check_every <= 0 && chunk < 128) chunk *= 2;
+        if (prof) {
+            int ran = h.iter - it0;
+            if (h.status == GBS_EBREAKDOWN || h.status == GBS_ENONFINITE) ++ran;  // K1 ran, K2 did not
+            for (int i = 0; i < ran && i < n; ++i) {
+                float ms = 0.0f;
+                GBS_CUDA_TRY(cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]));
+                prof->seconds += 1e-3 * ms;
+                prof->launches += 1;
+            }
+        }
+        if (check_every <= 0 && chunk < max_chunk) chunk *= 2;
     }
+    for (auto &e : ev) cudaEventDestroy(e);
     pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc);
     GBS_LAUNCH_CHECK("pcg_finalize_kernel");
     rc = read_scalars(w.sc, &h, st);
@@ -352,6 +380,7 @@ static int read_outer(const OuterScalars *d, OuterScalars *h, cudaStream_t st) {
 int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x, const double *f,
               const uint8_t *mask, double *u, const gbsimp_solve_opts *o, gbsimp_solve_stats *stats, void *ws,
               cudaStream_t st) {
+    ApplyProfile prof;
     const int64_t nd = n_dof_of(nx, ny, nz);
     SolveWs w = solve_ws(ws, nx, ny, nz);
     GBS_CUDA_TRY(cudaMemsetAsync(w.os, 0, sizeof(OuterScalars), st));
@@ -392,7 +421,7 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
         if (itol < inner) itol = inner;
         PcgScalars ps;
         rc = pcg_run(ctx, nx, ny, nz, law, x, w.b32, mask, w.d32, itol, o->max_iter - total, o->check_every, w.pcg,
-                     &ps, st);
+                     &ps, st, o->profile ? &prof : nullptr);
         if (rc) return rc;
         total += ps.iter;
         if (ps.status == GBS_EBREAKDOWN || ps.status == GBS_ENONFINITE) {
@@ -408,6 +437,8 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
         stats->iterations = total;
         stats->outer = outer;
         stats->relres = relres;
+        stats->apply_seconds = prof.seconds;
+        stats->apply_launches = prof.launches;
     }
     return GBS_OK;
 }
@@ -583,10 +614,13 @@ extern "C" int gbsimp_pcg_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbs
         return set_error(GBS_EINVAL, "gbsimp_pcg_f32: bad arguments");
     if (ws_bytes < pcg_ws_bytes_impl(nx, ny, nz)) return set_error(GBS_EINVAL, "gbsimp_pcg_f32: workspace too small");
     PcgScalars h;
+    ApplyProfile prof;
     int rc = pcg_run(ctx, nx, ny, nz, law, x, b, node_mask, u, opts->rtol, opts->max_iter, opts->check_every, ws, &h,
-                     (cudaStream_t)stream);
+                     (cudaStream_t)stream, opts->profile ? &prof : nullptr);
     if (rc) return rc;
     if (stats) {
+        stats->apply_seconds = prof.seconds;
+        stats->apply_launches = prof.launches;
         stats->status = h.status;
         stats->iterations = h.iter;
         stats->outer = 0;
@@ -640,6 +674,7 @@ extern "C" int gbsimp_pcg_csr_f32(gbsimp_ctx *ctx, int64_t n, const int32_t *row
     if (n_fixed > 0) zero_list_kernel<<<fb, 256, 0, st>>>(n_fixed, fixed, n, w.r);
     csr_z_kernel<<<vb, 256, 0, st>>>(n, w.r, diagonal, w.z, w.p, 1, w.partials, w.sc);
     csr_p_kernel<<<vb, 256, 0, st>>>(n, w.z, w.p, 1, w.sc);
+    count_launches(4);
     GBS_LAUNCH_CHECK("csr setup");
     const int chunk = opts->check_every > 0 ? opts->check_every : 32;
     CsrScalars h{};
@@ -656,6 +691,7 @@ extern "C" int gbsimp_pcg_csr_f32(gbsimp_ctx *ctx, int64_t n, const int32_t *row
             csr_z_kernel<<<vb, 256, 0, st>>>(n, w.r, diagonal, w.z, w.p, 0, w.partials, w.sc);
             csr_p_kernel<<<vb, 256, 0, st>>>(n, w.z, w.p, 0, w.sc);
         }
+        count_launches(8 * m - 1);
         GBS_LAUNCH_CHECK("csr iteration");
         launched += m;
         GBS_CUDA_TRY(cudaMemcpyAsync(hp, w.sc, sizeof h, cudaMemcpyDeviceToHost, st));

@@ -1,0 +1,283 @@
+"""Device engine: one gbsimp context plus caller-owned workspaces, driven with torch tensors.
+
+All array arguments are contiguous torch CUDA tensors in the reference layout; every call
+is ordered on torch's current CUDA stream. Workspaces are torch allocations owned by the
+engine (grow-only, keyed by purpose), so the library itself never allocates device memory.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from typing import Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+Grid = Sequence[int]
+
+
+def _p(t: Optional[torch.Tensor]):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _need(t: torch.Tensor, dtype, n: int, name: str):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name}: expected a CUDA tensor")
+    if t.dtype != dtype:
+        raise TypeError(f"{name}: expected {dtype}, got {t.dtype}")
+    if not t.is_contiguous() or t.numel() != n:
+        raise ValueError(f"{name}: expected a contiguous tensor of {n} entries, got {tuple(t.shape)}")
+
+
+def n_elem(grid: Grid) -> int:
+    nx, ny, nz = grid
+    return nx * ny * nz
+
+
+def n_dof(grid: Grid) -> int:
+    nx, ny, nz = grid
+    return 3 * (nx + 1) * (ny + 1) * (nz + 1)
+
+
+class Engine:
+    """One gbsimp context on one CUDA device."""
+
+    def __init__(self, device: Optional[torch.device] = None, ke: Optional[np.ndarray] = None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("genpipeline_gb300 needs a CUDA GPU; there is no CPU fallback")
+        self.lib = L.load()
+        self.device = torch.device(device if device is not None else "cuda", )
+        if self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            L.check(self.lib.gbsimp_create(C.byref(h)))
+        self.ctx = h
+        self._ws = {}
+        if ke is not None:
+            self.set_ke(ke)
+
+    def __del__(self):
+        try:
+            if getattr(self, "ctx", None):
+                self.lib.gbsimp_destroy(self.ctx)
+                self.ctx = None
+        except Exception:
+            pass
+
+    # ---- element stiffness -------------------------------------------------------------
+    def set_ke(self, ke) -> None:
+        k = np.ascontiguousarray(np.asarray(ke, dtype=np.float64).reshape(576))
+        L.check(self.lib.gbsimp_set_ke(self.ctx, k.ctypes.data_as(C.POINTER(C.c_double))))
+
+    def get_ke(self) -> np.ndarray:
+        k = np.empty(576)
+        L.check(self.lib.gbsimp_get_ke(self.ctx, k.ctypes.data_as(C.POINTER(C.c_double))))
+        return k.reshape(24, 24)
+
+    @staticmethod
+    def ke_quadrature(nu=0.3, e0=1.0) -> np.ndarray:
+        k = np.empty(576)
+        L.check(L.load().gbsimp_ke_quadrature(float(nu), float(e0), k.ctypes.data_as(C.POINTER(C.c_double))))
+        return k.reshape(24, 24)
+
+    # ---- workspaces ---------------------------------------------------------------------
+    def workspace(self, key: str, nbytes: int) -> torch.Tensor:
+        """Grow-only scratch buffer per (host thread, purpose): threads that share an engine
+        never share scratch memory."""
+        k = (threading.get_ident(), key)
+        t = self._ws.get(k)
+        if t is None or t.numel() < nbytes:
+            t = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=self.device)
+            self._ws[k] = t
+        return t
+
+    # ---- kernels ------------------------------------------------------------------------
+    def apply(self, grid: Grid, law: L.Law, x: torch.Tensor, p: torch.Tensor,
+              mask: Optional[torch.Tensor] = None, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        nx, ny, nz = grid
+        nd = n_dof(grid)
+        _need(x, torch.float32, n_elem(grid), "x")
+        if p.dtype not in (torch.float32, torch.float64):
+            raise TypeError("p must be float32 or float64")
+        _need(p, p.dtype, nd, "p")
+        if mask is not None:
+            _need(mask, torch.uint8, nd // 3, "mask")
+        y = torch.empty_like(p) if out is None else out
+        fn = self.lib.gbsimp_apply_f32 if p.dtype == torch.float32 else self.lib.gbsimp_apply_f64
+        L.check(fn(self.ctx, nx, ny, nz, C.byref(law), _p(x), _p(p), _p(y), _p(mask), _stream()))
+        return y
+
+    def apply_edof(self, law: L.Law, x: torch.Tensor, p: torch.Tensor, edof: torch.Tensor) -> torch.Tensor:
+        ne = edof.shape[0]
+        if edof.dim() != 2 or edof.shape[1] != 24 or edof.dtype not in (torch.int32, torch.int64):
+            raise ValueError("edof must be an (n_elem, 24) int32/int64 tensor")
+        edof = edof.contiguous()
+        _need(x, torch.float32, ne, "x")
+        _need(p, torch.float32, p.numel(), "p")
+        y = torch.empty_like(p)
+        L.check(self.lib.gbsimp_apply_edof_f32(self.ctx, ne, p.numel(), _p(edof), int(edof.dtype == torch.int64),
+                                                C.byref(law), _p(x), _p(p), _p(y), _stream()))
+        return y
+
+    def sensitivity(self, grid: Grid, law: L.Law, x: torch.Tensor, u: torch.Tensor, dc: Optional[torch.Tensor] = None,
+                    ce: Optional[torch.Tensor] = None, energy: Optional[torch.Tensor] = None):
+        """dc (float32), optional ce, optional energy (device float64 scalar tensor)."""
+        nx, ny, nz = grid
+        _need(x, torch.float32, n_elem(grid), "x")
+        _need(u, torch.float64, n_dof(grid), "u")
+        if dc is None:
+            dc = torch.empty(n_elem(grid), dtype=torch.float32, device=x.device)
+        nb = self.lib.gbsimp_sensitivity_ws_bytes(nx, ny, nz)
+        ws = self.workspace("sens", nb)
+        L.check(self.lib.gbsimp_sensitivity(self.ctx, nx, ny, nz, C.byref(law), _p(x), _p(u), _p(dc), _p(ce),
+                                             _p(energy), _p(ws), nb, _stream()))
+        return dc
+
+    def sensitivity_edof(self, law: L.Law, x: torch.Tensor, u: torch.Tensor, edof: torch.Tensor) -> torch.Tensor:
+        ne = edof.shape[0]
+        edof = edof.contiguous()
+        _need(x, torch.float32, ne, "x")
+        _need(u, torch.float32, u.numel(), "u")
+        dc = torch.empty(ne, dtype=torch.float32, device=x.device)
+        L.check(self.lib.gbsimp_sensitivity_edof_f32(self.ctx, ne, u.numel(), _p(edof),
+                                                      int(edof.dtype == torch.int64), C.byref(law), _p(x), _p(u),
+                                                      _p(dc), _stream()))
+        return dc
+
+    def filter_hs(self, grid: Grid, rmin: float) -> torch.Tensor:
+        nx, ny, nz = grid
+        hs = torch.empty(n_elem(grid), dtype=torch.float32, device=self.device)
+        L.check(self.lib.gbsimp_filter_hs(self.ctx, nx, ny, nz, float(rmin), _p(hs), _stream()))
+        return hs
+
+    def filter(self, grid: Grid, rmin: float, v: torch.Tensor, hs: Optional[torch.Tensor] = None,
+               transpose: bool = False, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        nx, ny, nz = grid
+        _need(v, torch.float32, n_elem(grid), "v")
+        if transpose and hs is None:
+            hs = self.filter_hs(grid, rmin)
+        o = torch.empty_like(v) if out is None else out
+        L.check(self.lib.gbsimp_filter(self.ctx, nx, ny, nz, float(rmin), _p(hs), _p(v), _p(o), int(bool(transpose)),
+                                       _stream()))
+        return o
+
+    def oc_workspace(self, grid: Grid, key: str = "oc") -> torch.Tensor:
+        nx, ny, nz = grid
+        return self.workspace(key, self.lib.gbsimp_oc_ws_bytes(nx, ny, nz))
+
+    def oc_prepare(self, grid: Grid, rmin: float, preserved: Optional[torch.Tensor] = None, key: str = "oc"):
+        nx, ny, nz = grid
+        ws = self.oc_workspace(grid, key)
+        if preserved is not None:
+            _need(preserved, torch.uint8, n_elem(grid), "preserved")
+        L.check(self.lib.gbsimp_oc_prepare(self.ctx, nx, ny, nz, float(rmin), _p(preserved), _p(ws), ws.numel(),
+                                           _stream()))
+        return ws
+
+    def oc(self, grid: Grid, rmin: float, volfrac: float, x: torch.Tensor, dc: torch.Tensor,
+           preserved: Optional[torch.Tensor] = None, variant=None, xnew=None, xphys=None, key: str = "oc",
+           prepared: bool = False):
+        nx, ny, nz = grid
+        n = n_elem(grid)
+        _need(x, torch.float32, n, "x")
+        _need(dc, torch.float32, n, "dc")
+        ws = self.oc_workspace(grid, key) if prepared else self.oc_prepare(grid, rmin, preserved, key)
+        xnew = torch.empty_like(x) if xnew is None else xnew
+        xphys = torch.empty_like(x) if xphys is None else xphys
+        prm = L.make_oc(volfrac, variant)
+        L.check(self.lib.gbsimp_oc(self.ctx, nx, ny, nz, float(rmin), C.byref(prm), _p(x), _p(dc), _p(preserved),
+                                   _p(xnew), _p(xphys), _p(ws), ws.numel(), _stream()))
+        return xnew, xphys
+
+    def oc_result(self, key: str = "oc"):
+        lam = C.c_double()
+        steps = C.c_int()
+        L.check(self.lib.gbsimp_oc_result(self.ctx, _p(self._ws[(threading.get_ident(), key)]), C.byref(lam), C.byref(steps), _stream()))
+        return lam.value, steps.value
+
+    @staticmethod
+    def opts(rtol=1e-8, inner_rtol=1e-3, max_iter=20000, max_outer=20, check_every=0, fused=0,
+             profile=0) -> L.SolveOpts:
+        return L.SolveOpts(float(rtol), float(inner_rtol), int(max_iter), int(max_outer), int(check_every),
+                           int(fused), int(profile), 0)
+
+    def pcg(self, grid: Grid, law: L.Law, x: torch.Tensor, b: torch.Tensor, mask: Optional[torch.Tensor],
+            u: torch.Tensor, rtol=1e-6, max_iter=2000, check_every=0, key: str = "pcg", profile=False) -> dict:
+        nx, ny, nz = grid
+        nd = n_dof(grid)
+        _need(x, torch.float32, n_elem(grid), "x")
+        _need(b, torch.float32, nd, "b")
+        _need(u, torch.float32, nd, "u")
+        nb = self.lib.gbsimp_pcg_ws_bytes(nx, ny, nz)
+        ws = self.workspace(key, nb)
+        st = L.SolveStats()
+        o = self.opts(rtol=rtol, max_iter=max_iter, check_every=check_every, profile=int(profile))
+        L.check(self.lib.gbsimp_pcg_f32(self.ctx, nx, ny, nz, C.byref(law), _p(x), _p(b), _p(mask), _p(u), C.byref(o),
+                                        C.byref(st), _p(ws), nb, _stream()))
+        return st.as_dict()
+
+    def solve(self, grid: Grid, law: L.Law, x: torch.Tensor, f: torch.Tensor, mask: Optional[torch.Tensor],
+              u: torch.Tensor, rtol=1e-8, inner_rtol=1e-3, max_iter=100000, max_outer=30, check_every=0,
+              key: str = "solve", profile=False) -> dict:
+        nx, ny, nz = grid
+        nd = n_dof(grid)
+        _need(x, torch.float32, n_elem(grid), "x")
+        _need(f, torch.float64, nd, "f")
+        _need(u, torch.float64, nd, "u")
+        nb = self.lib.gbsimp_solve_ws_bytes(nx, ny, nz)
+        ws = self.workspace(key, nb)
+        st = L.SolveStats()
+        o = self.opts(rtol=rtol, inner_rtol=inner_rtol, max_iter=max_iter, max_outer=max_outer,
+                      check_every=check_every, profile=int(profile))
+        L.check(self.lib.gbsimp_solve(self.ctx, nx, ny, nz, C.byref(law), _p(x), _p(f), _p(mask), _p(u), C.byref(o),
+                                      C.byref(st), _p(ws), nb, _stream()))
+        return st.as_dict()
+
+    def pcg_csr(self, row_ptr, col_idx, values, diagonal, b, x, fixed, rtol=1e-6, max_iter=100) -> dict:
+        n = b.numel()
+        _need(b, torch.float32, n, "b")
+        _need(x, torch.float32, n, "x")
+        _need(diagonal, torch.float32, n, "diagonal")
+        _need(row_ptr, torch.int32, n + 1, "row_ptr")
+        _need(col_idx, torch.int32, col_idx.numel(), "col_idx")
+        _need(values, torch.float32, col_idx.numel(), "values")
+        nf = 0 if fixed is None else fixed.numel()
+        if fixed is not None:
+            _need(fixed, torch.int32, nf, "fixed")
+        nb = self.lib.gbsimp_pcg_csr_ws_bytes(n)
+        ws = self.workspace("csr", nb)
+        st = L.SolveStats()
+        o = self.opts(rtol=rtol, max_iter=max_iter)
+        L.check(self.lib.gbsimp_pcg_csr_f32(self.ctx, n, _p(row_ptr), _p(col_idx), _p(values), _p(diagonal), _p(b),
+                                            _p(x), _p(fixed), nf, C.byref(o), C.byref(st), _p(ws), nb, _stream()))
+        return st.as_dict()
+
+    def dot64(self, a: torch.Tensor, b: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        _need(a, torch.float64, a.numel(), "a")
+        _need(b, torch.float64, a.numel(), "b")
+        o = torch.empty((), dtype=torch.float64, device=a.device) if out is None else out
+        nb = 256 + 4096 * 32
+        ws = self.workspace("dot", nb)
+        L.check(self.lib.gbsimp_dot_f64(self.ctx, a.numel(), _p(a), _p(b), _p(o), _p(ws), nb, _stream()))
+        return o
+
+
+_ENGINES = {}
+
+
+def get_engine(device=None) -> Engine:
+    """Process-wide engine per device (the library context is re-entrant across streams)."""
+    dev = torch.device(device if device is not None else "cuda")
+    idx = dev.index if dev.index is not None else torch.cuda.current_device()
+    e = _ENGINES.get(idx)
+    if e is None:
+        e = Engine(torch.device("cuda", idx))
+        _ENGINES[idx] = e
+    return e

@@ -70,6 +70,8 @@ typedef struct gbsimp_solve_opts {
     int32_t max_outer;    /* cap on FP64 defect corrections (gbsimp_solve only) */
     int32_t check_every;  /* iterations between host-side convergence checks (0 = auto) */
     int32_t fused;        /* 1 = persistent fused PCG kernel, 0 = one launch per step */
+    int32_t profile;      /* 1 = time every PCG apply launch with CUDA events (stats) */
+    int32_t reserved;
 } gbsimp_solve_opts;
 
 typedef struct gbsimp_solve_stats {
@@ -79,12 +81,17 @@ typedef struct gbsimp_solve_stats {
     int32_t reserved;
     double relres;        /* last ||D(f - K u)|| / ||D f|| */
     double seconds;       /* host wall time of the call */
+    double apply_seconds; /* device time of the PCG apply launches (opts->profile only) */
+    int32_t apply_launches;
+    int32_t reserved2;
 } gbsimp_solve_stats;
 
 typedef struct gbsimp_ctx gbsimp_ctx;
 
 /* ---- context ---------------------------------------------------------------------- */
 int gbsimp_abi_version(void);
+/* Number of CUDA kernels this library has launched in the process (all threads). */
+uint64_t gbsimp_launch_count(void);
 const char *gbsimp_last_error(void);
 /* Creates a context bound to the current CUDA device, holding the quadrature element
  * stiffness of (nu = 0.3, E = 1). No device memory is allocated. */

@@ -1,0 +1,61 @@
+"""CPU checks of the C ABI: the library builds/loads and exports every declared symbol;
+host-only entry points work without a GPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from genpipeline_gb300 import _lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(gbsimp_\w+)\s*\(", src))
+    return names
+
+
+def test_every_declared_symbol_is_exported_and_bound():
+    lib = L.load()
+    names = _declared()
+    assert len(names) >= 25
+    for n in sorted(names):
+        assert hasattr(lib, n), n
+    # the Python binding covers the whole header
+    assert names <= set(L.SIGNATURES), sorted(names - set(L.SIGNATURES))
+
+
+def test_abi_version_and_errors():
+    lib = L.load()
+    assert lib.gbsimp_abi_version() == 1
+    with pytest.raises(L.GbsimpError) as ei:
+        L.check(lib.gbsimp_ke_quadrature(0.6, 1.0, None))
+    assert ei.value.code == L.GBS_EINVAL
+
+
+def test_library_ke_matches_oracle_and_reference_quadrature(golden):
+    from oracle import oracle as O
+    from genpipeline_gb300.engine import Engine
+
+    k = Engine.ke_quadrature(0.3, 1.0)
+    np.testing.assert_allclose(k, O.ke_quadrature(0.3), rtol=0, atol=2e-16)
+    np.testing.assert_allclose(k, golden("ke")["ke_quadrature"], rtol=0, atol=2e-16)
+    k2 = Engine.ke_quadrature(0.25, 2.0)
+    np.testing.assert_allclose(k2, O.ke_quadrature(0.25, 2.0), rtol=0, atol=1e-15)
+
+
+def test_workspace_queries_are_host_only():
+    lib = L.load()
+    for grid in ((1, 1, 1), (64, 64, 64), (192, 96, 96)):
+        nd = 3 * (grid[0] + 1) * (grid[1] + 1) * (grid[2] + 1)
+        assert lib.gbsimp_pcg_ws_bytes(*grid) >= 5 * 4 * nd
+        assert lib.gbsimp_solve_ws_bytes(*grid) >= lib.gbsimp_pcg_ws_bytes(*grid) + 16 * nd
+        assert lib.gbsimp_oc_ws_bytes(*grid) >= 8 * grid[0] * grid[1] * grid[2]
+    assert lib.gbsimp_pcg_csr_ws_bytes(1000) >= 16000
