@@ -33,12 +33,22 @@ sys.path.insert(0, ROOT)
 
 METRIC = "64^3 SIMP iters/s & FEM solves/s, served vs plain (1×GB300, rel err ≤1e-6); p50/p99"
 UNIT = "SIMP iterations/s"
-GRID = (64, 64, 64)
-WORKLOAD = {"workload": "simp_64cube_top_patch", "grid": list(GRID), "elements": 262144, "dofs": 823875,
-            "penal": 3.0, "rmin": 2.0, "volfrac": 0.25, "law": "E = 1e-9 + x^3 (1 - 1e-9)",
-            "load": "z=0 clamped, -z traction (total 1) on the central 16x16 top-face patch",
-            "solver": "FP32 Jacobi-PCG inner, FP64 defect correction to rtol 1e-8, warm start",
-            "oc": "bisection l1=0 l2=1e9 tol 1e-4 move 0.2 (SIMPSolver._oc_update)"}
+WORKLOADS = {
+    # the bench line: 64^3 SIMP (262,144 elements, 823,875 DOFs)
+    "simp64": {"workload": "simp_64cube_top_patch", "grid": [64, 64, 64], "rmin": 2.0, "volfrac": 0.25,
+               "load": "top_patch",
+               "load_text": "z=0 clamped, -z traction (total 1) on the central 16x16 top-face patch"},
+    # 32x16x16 cantilever (8,192 elements, 28,611 DOFs), for profiling and comparison
+    "c0": {"workload": "simp_32x16x16_cantilever", "grid": [32, 16, 16], "rmin": 1.5, "volfrac": 0.3,
+           "load": "cantilever", "load_text": "x=0 clamped, unit -z point load at node (32, 8, 0)"},
+    # 192x96x96 (1,769,472 elements, 5,447,811 DOFs): the HBM-bound size of the apply
+    "c4": {"workload": "simp_192x96x96_edge_line", "grid": [192, 96, 96], "rmin": 3.0, "volfrac": 0.2,
+           "load": "edge_line",
+           "load_text": "x=0 clamped, -z line load (total 1) along the bottom edge of the x=192 face"},
+}
+COMMON = {"penal": 3.0, "law": "E = 1e-9 + x^3 (1 - 1e-9)",
+          "solver": "FP32 Jacobi-PCG inner, FP64 defect correction to rtol 1e-8, warm start",
+          "oc": "bisection l1=0 l2=1e9 tol 1e-4 move 0.2 (SIMPSolver._oc_update)"}
 
 
 def _args():
@@ -47,21 +57,34 @@ def _args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="simp64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-steps", type=int, default=1)
+    ap.add_argument("--host-loop", action="store_true",
+                    help="launch PCG iterations from the host (for kernel profilers) instead of the graph loop")
     return ap.parse_args()
 
 
-def _spec():
+def _wl(a):
+    w = WORKLOADS[a.workload]
+    g = tuple(w["grid"])
+    cfg = {"workload": w["workload"], "grid": list(g), "elements": g[0] * g[1] * g[2],
+           "dofs": 3 * (g[0] + 1) * (g[1] + 1) * (g[2] + 1), "rmin": w["rmin"], "volfrac": w["volfrac"],
+           "load": w["load_text"], **COMMON}
+    return w, g, cfg
+
+
+def _spec(w):
     from genpipeline_gb300.simp import SolveSpec
 
-    return SolveSpec(grid=GRID, penal=3.0, rmin=2.0, volfrac=0.25, law="modified", rtol=1e-8, inner_rtol=1e-3)
+    return SolveSpec(grid=tuple(w["grid"]), penal=3.0, rmin=w["rmin"], volfrac=w["volfrac"], law="modified",
+                     rtol=1e-8, inner_rtol=1e-3)
 
 
-def _load_case():
+def _load_case(w):
     from genpipeline_gb300 import bcs
 
-    return bcs.top_patch(*GRID)
+    return bcs.LOAD_CASES[w["load"]](*w["grid"])
 
 
 # ---- clocks ------------------------------------------------------------------------------
@@ -172,9 +195,11 @@ def run_ours(a):
         dist.init_process_group("nccl", init_method="env://")
     dev = torch.device("cuda", torch.cuda.current_device())
     lib = L.load()
-    spec = _spec()
-    f, fixed = _load_case()
+    w, GRID, WORKLOAD = _wl(a)
+    spec = _spec(w)
+    f, fixed = _load_case(w)
     prob = SimpProblem(spec, f, fixed, device=dev)
+    prob.profile = bool(a.host_loop)
     nd, ne = prob.f.numel(), prob.x.numel()
     flush = torch.empty(256 * 2**20, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
 
@@ -188,7 +213,6 @@ def run_ours(a):
     barrier()
     clocks = ClockSampler(dev.index if dev.index is not None else 0)
     clocks.start()
-    prob.profile = True
     launches0 = lib.gbsimp_launch_count()
     st0 = torch.cuda.Event(enable_timing=True)
     st1 = torch.cuda.Event(enable_timing=True)
@@ -202,7 +226,6 @@ def run_ours(a):
     barrier()
     launches = lib.gbsimp_launch_count() - launches0  # our kernels only (the L2 flush is torch)
     clk = clocks.stop()
-    prob.profile = False
     t = st0.elapsed_time(st1) * 1e-3
     tmax = t
     if world > 1:
@@ -211,8 +234,9 @@ def run_ours(a):
         tmax = float(tt.item())
     value = world * a.steps / tmax
     pcg_iters = sum(s["iterations"] for s in stats)
-    apply_s = sum(s["apply_seconds"] for s in stats)
-    apply_n = sum(s["apply_launches"] for s in stats)
+    # The dominant kernel, timed live on the final density field of the timed region:
+    # 50 back-to-back launches replayed from a CUDA graph, CUDA events on this stream.
+    per_launch = prob.eng.time_pcg_apply(GRID, prob.law, prob.xphys, prob.mask, reps=50)
 
     # ---- e2e: through the public API with host buffers --------------------------------
     # Each step takes the design x from pinned host memory and returns the updated design
@@ -242,16 +266,13 @@ def run_ours(a):
     # ---- roofline of the dominant kernel (the fused PCG apply, K1) ----------------------
     alg_bytes = 4 * (7 * nd + ne)  # r, dinv, p_old, x_u, x in; p_new, Ap, x_u out
     peak, peak_src = _measured_peak()
-    roof = None
-    if apply_n > 0:
-        per_launch = apply_s / apply_n
-        achieved = alg_bytes / per_launch / 1e9
-        roof = {"bound": "hbm", "kernel": "apply_tile_kernel<PCG> (fused K(x)p + p update + p.Ap)",
-                "achieved": achieved, "peak": peak, "peak_source": peak_src, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": _profiled_traffic(), "alg_bytes_per_launch": alg_bytes,
-                "launch_us": per_launch * 1e6, "launches": apply_n,
-                "fp32_tflops": 1152 * ne / per_launch / 1e12,
-                "share_of_step": apply_s / t}
+    achieved = alg_bytes / per_launch / 1e9
+    path = prob.eng.apply_path(GRID[2])
+    roof = {"bound": "hbm", "kernel": f"apply_{path}_kernel<PCG> (K(x)p fused with p = z + beta p, x update, p.Ap)",
+            "achieved": achieved, "peak": peak, "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": _profiled_traffic(), "alg_bytes_per_launch": alg_bytes, "launch_us": per_launch * 1e6,
+            "fp32_flops_per_launch_dense_equiv": 1152 * ne,
+            "est_share_of_step": pcg_iters * per_launch / t}
 
     # ---- CPU baseline: the oracle on the same trajectory, from the GPU's state ----------
     cpu = None
@@ -261,7 +282,8 @@ def run_ours(a):
         from oracle import oracle as O
 
         mat = O.Material("modified", 3.0, emin=1e-9)
-        ost = O.SimpState(GRID, O.ke_quadrature(), mat, 2.0, f, bcs.dof_mask(*GRID, fixed), 0.25, tol=1e-8)
+        ost = O.SimpState(GRID, O.ke_quadrature(), mat, w["rmin"], f, bcs.dof_mask(*GRID, fixed), w["volfrac"],
+                          tol=1e-8)
         ost.x = prob.x.double().cpu().numpy().copy()
         ost.xphys = prob.xphys.double().cpu().numpy().copy()
         ost.u = prob.u.cpu().numpy().copy()
@@ -278,7 +300,7 @@ def run_ours(a):
         tc = time.perf_counter() - c0
         rel_err = abs(c_gpu - c_cpu) / abs(c_cpu)
         cpu = {"value": a.cpu_sample_steps / tc, "unit": UNIT, "cores": _cpu_threads(), "kind": "port",
-               "sample": f"{a.cpu_sample_steps} OC iteration(s) of the same 64^3 trajectory, started from the "
+               "sample": f"{a.cpu_sample_steps} OC iteration(s) of the same trajectory, started from the "
                          f"GPU state after {a.warmup + 2 * a.steps} iterations (FP64 C/OpenMP oracle)",
                "seconds": tc}
 
@@ -287,8 +309,8 @@ def run_ours(a):
                 "warmup": a.warmup, "ms_per_step": tmax / a.steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 outer residual, dots, compliance)",
                 "data": "synthetic", "impl": "ours",
-                "config": dict(WORKLOAD, l2="L2 flushed (256 MB write) before every timed step; the 64^3 PCG "
-                                         "working set (~35 MB) is L2-resident inside a step",
+                "config": dict(WORKLOAD, l2="L2 flushed (256 MB write) before every timed step; inside a step "
+                                         "the PCG vectors stay in L2 when they fit (64^3: ~36 MB)",
                                parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clk, "pcg_iterations_per_step": pcg_iters / a.steps,
@@ -306,9 +328,11 @@ def run_reference(a):
     from genpipeline_gb300 import bcs
     from oracle import oracle as O
 
-    f, fixed = _load_case()
+    w, GRID, WORKLOAD = _wl(a)
+    f, fixed = _load_case(w)
     mat = O.Material("modified", 3.0, emin=1e-9)
-    st = O.SimpState(GRID, O.ke_quadrature(), mat, 2.0, f, bcs.dof_mask(*GRID, fixed), 0.25, tol=1e-8)
+    st = O.SimpState(GRID, O.ke_quadrature(), mat, w["rmin"], f, bcs.dof_mask(*GRID, fixed), w["volfrac"],
+                     tol=1e-8)
     for _ in range(a.warmup):
         st.step()
     t0 = time.perf_counter()
@@ -322,7 +346,7 @@ def run_reference(a):
             "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": dict(WORKLOAD, solver="FP64 Jacobi-PCG to rtol 1e-8, warm start (oracle port)"),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"OC iterations {a.warmup}..{a.warmup + a.steps - 1} of the 64^3 trajectory "
+                             "sample": f"OC iterations {a.warmup}..{a.warmup + a.steps - 1} of the trajectory "
                                        "(FP64 C/OpenMP restatement of SIMPSolver, all host threads)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

@@ -84,6 +84,7 @@ SIGNATURES = {
     "gbsimp_set_ke": (_I, [_P, C.POINTER(_D)]),
     "gbsimp_get_ke": (_I, [_P, C.POINTER(_D)]),
     "gbsimp_apply_f32": (_I, [_P, _I, _I, _I, C.POINTER(Law), _P, _P, _P, _P, _P]),
+    "gbsimp_apply_path": (_I, [_P, _I]),
     "gbsimp_apply_f64": (_I, [_P, _I, _I, _I, C.POINTER(Law), _P, _P, _P, _P, _P]),
     "gbsimp_apply_edof_f32": (_I, [_P, _I64, _I64, _P, _I, C.POINTER(Law), _P, _P, _P, _P]),
     "gbsimp_sensitivity_ws_bytes": (_SZ, [_I, _I, _I]),
@@ -98,6 +99,8 @@ SIGNATURES = {
     "gbsimp_pcg_ws_bytes": (_SZ, [_I, _I, _I]),
     "gbsimp_pcg_f32": (_I, [_P, _I, _I, _I, C.POINTER(Law), _P, _P, _P, _P, C.POINTER(SolveOpts),
                             C.POINTER(SolveStats), _P, _SZ, _P]),
+    "gbsimp_time_pcg_apply_ws_bytes": (_SZ, [_I, _I, _I]),
+    "gbsimp_time_pcg_apply": (_I, [_P, _I, _I, _I, C.POINTER(Law), _P, _P, _I, _P, _SZ, C.POINTER(_D), _P]),
     "gbsimp_solve_ws_bytes": (_SZ, [_I, _I, _I]),
     "gbsimp_solve": (_I, [_P, _I, _I, _I, C.POINTER(Law), _P, _P, _P, _P, C.POINTER(SolveOpts),
                           C.POINTER(SolveStats), _P, _SZ, _P]),

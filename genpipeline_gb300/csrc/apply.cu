@@ -1,5 +1,5 @@
 // apply.cu -- C-ABI entry points of the element stiffness apply y = D K(x) D p.
-#include "apply_tile.cuh"
+#include "apply_modal.cuh"
 #include "internal.h"
 
 namespace gbs {
@@ -20,6 +20,8 @@ int launch_apply_plain(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<
 
 int apply_f32(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
               const float *p, float *y, const uint8_t *mask, cudaStream_t st) {
+    if (ctx->modal_ok && modal_fits(nz))
+        return launch_modal<MODE_PLAIN>(ctx, nx, ny, nz, make_law<float>(*law), x, p, y, mask, PcgArgs{}, st);
     return launch_apply_plain<TileF, float, KeF>(ctx, nx, ny, nz, make_law<float>(*law), ctx->kef, x, p, y, mask,
                                                  st);
 }
@@ -97,6 +99,11 @@ extern "C" int gbsimp_apply_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const g
     if (!ctx || !law || !x || !p || !y || nx <= 0 || ny <= 0 || nz <= 0)
         return set_error(GBS_EINVAL, "gbsimp_apply_f32: bad arguments");
     return apply_f32(ctx, nx, ny, nz, law, x, p, y, node_mask, (cudaStream_t)stream);
+}
+
+extern "C" int gbsimp_apply_path(const gbsimp_ctx *ctx, int nz) {
+    if (!ctx) return -1;
+    return (ctx->modal_ok && modal_fits(nz)) ? 1 : 0;
 }
 
 extern "C" int gbsimp_apply_f64(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,

@@ -36,6 +36,8 @@ struct PcgScalars {
     int status;       // GBS_OK / GBS_ENOTCONV / GBS_EBREAKDOWN / GBS_ENONFINITE
     int max_iter;
     unsigned counter; // blocks finished in the running kernel (last-block reductions)
+    int trips;        // WHILE-loop trips run by the device-driven loop
+    int max_trips;    // hard cap on those trips (the loop always ends)
     int pad;
 };
 

@@ -14,7 +14,14 @@ namespace gbs {
 static thread_local char g_err[512] = "";
 static std::atomic<unsigned long long> g_launches{0};
 
-void count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
+static thread_local bool g_capturing = false;
+
+// Launches enqueued while a graph is being captured are not executions; graph replays add
+// their kernel count explicitly.
+void count_launches(int n) {
+    if (!g_capturing && n > 0) g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed);
+}
+void set_capturing(bool on) { g_capturing = on; }
 
 int set_error(int code, const char *fmt, ...) {
     va_list ap;
@@ -89,6 +96,7 @@ void *thread_pinned() {
 }
 
 static void install_ke(gbsimp_ctx *ctx, const double *ke) {
+    ctx->ke_version += 1;
     double mx = 0.0, tr = 0.0;
     for (int i = 0; i < 576; ++i) {
         ctx->ke[i] = ke[i];
@@ -104,6 +112,46 @@ static void install_ke(gbsimp_ctx *ctx, const double *ke) {
             tr = fmax(tr, fabs(s));
         }
     ctx->translation_free = mx > 0.0 && tr <= 1e-12 * mx;
+    // Modal form Km = T^T Ke T / 64 (T = T8 (x) I3, T8[a][m] = prod_d (m_d ? s(c_d(a)) : 1),
+    // modes bit-ordered (x, y, z) = (4, 2, 1)); usable when Ke has no entry outside the
+    // 45-entry pattern of an isotropic cube element.
+    {
+        double T8[8][8];
+        for (int a = 0; a < 8; ++a)
+            for (int m = 0; m < 8; ++m) {
+                double v = 1.0;
+                const int c[3] = {kCorner[a][0], kCorner[a][1], kCorner[a][2]};
+                const int mb[3] = {(m >> 2) & 1, (m >> 1) & 1, m & 1};
+                for (int d = 0; d < 3; ++d)
+                    if (mb[d]) v *= c[d] ? 1.0 : -1.0;
+                T8[a][m] = v;
+            }
+        double km[24][24];
+        double kmax = 0.0;
+        for (int r = 0; r < 24; ++r)
+            for (int cc = 0; cc < 24; ++cc) {
+                double s = 0.0;
+                for (int a = 0; a < 8; ++a)
+                    for (int b = 0; b < 8; ++b)
+                        s += T8[a][r / 3] * ke[(3 * a + r % 3) * 24 + 3 * b + cc % 3] * T8[b][cc / 3];
+                km[r][cc] = s / 64.0;
+                kmax = fmax(kmax, fabs(km[r][cc]));
+            }
+        bool in_pattern[24][24] = {};
+        for (int i = 0; i < kModalNnz; ++i) {
+            in_pattern[modal_row(i)][modal_col(i)] = true;
+            ctx->km.v[i] = (float)km[modal_row(i)][modal_col(i)];
+            ctx->kmd.v[i] = km[modal_row(i)][modal_col(i)];
+        }
+        bool ok = kmax > 0.0;
+        for (int r = 0; r < 24 && ok; ++r)
+            for (int cc = 0; cc < 24; ++cc)
+                if (!in_pattern[r][cc] && fabs(km[r][cc]) > 1e-12 * kmax) {
+                    ok = false;
+                    break;
+                }
+        ctx->modal_ok = ok;
+    }
     for (int i = 0; i < 24; ++i) {
         ctx->ke_diag_d[i] = ke[i * 25];
         ctx->ke_diag_f[i] = (float)ke[i * 25];
@@ -145,12 +193,14 @@ extern "C" int gbsimp_create(gbsimp_ctx **out) {
     double ke[576];
     ke_quadrature(0.3, 1.0, ke);
     install_ke(c, ke);
+    c->graphs = graph_cache_create();
     *out = c;
     return GBS_OK;
 }
 
 extern "C" int gbsimp_destroy(gbsimp_ctx *ctx) {
     if (!ctx) return GBS_OK;
+    graph_cache_destroy(ctx->graphs);
     free(ctx);
     return GBS_OK;
 }

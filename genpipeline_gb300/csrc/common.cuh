@@ -121,6 +121,28 @@ __device__ __forceinline__ double block_sum(double v, double *scratch) {
     return r;
 }
 
+constexpr int kModalNnz = 45;
+
+// Modal form of the isotropic cube element (see apply_modal.cuh). Sparsity pattern of Km in (mode*3 + component) indices (derived from the quadrature
+// element; capi.cu checks that the installed Ke has no entry outside it).
+__host__ __device__ constexpr int modal_row(int i) {
+    constexpr int r[kModalNnz] = {3,  3,  4,  4,  5,  5,  5,  6,  6,  7,  7,  7,  8,  8,  9,  9,  9,  10, 10, 11, 11, 12, 12,
+                                  12, 13, 13, 14, 14, 15, 15, 16, 16, 16, 17, 17, 18, 18, 19, 19, 20, 20, 20, 21, 22, 23};
+    return r[i];
+}
+__host__ __device__ constexpr int modal_col(int i) {
+    constexpr int c[kModalNnz] = {3, 14, 4,  8,  5,  7,  12, 6,  13, 5,  7,  12, 4,  8,  9,  16, 20, 10, 15, 11, 18, 5, 7,
+                                  12, 6, 13, 3, 14, 10, 15, 9,  16, 20, 17, 19, 11, 18, 17, 19, 9,  16, 20, 21, 22, 23};
+    return c[i];
+}
+
+struct ModalK {
+    float v[kModalNnz];
+};
+struct ModalKD {
+    double v[kModalNnz];
+};
+
 }  // namespace gbs
 
 // ---- library-internal host helpers (capi.cu) -------------------------------------------
@@ -133,12 +155,20 @@ struct gbsimp_ctx {
     float ke_diag_f[24];
     double ke_diag_d[24];
     int num_sms;
+    bool modal_ok;          // Ke has the modal sparsity of an isotropic cube element
+    gbs::ModalK km;         // its 45 modal coefficients (Km / 64)
+    gbs::ModalKD kmd;       // the same in FP64
+    unsigned ke_version;    // bumped by every set_ke (keys the graph cache)
+    void *graphs;           // gbs::GraphCache* (pcg.cu): instantiated device-loop graphs
 };
 
 namespace gbs {
 int set_error(int code, const char *fmt, ...);
 int cuda_error(cudaError_t e, const char *what);
 void count_launches(int n);
+void set_capturing(bool on);
+void *graph_cache_create();
+void graph_cache_destroy(void *gc);
 }  // namespace gbs
 
 #define GBS_CUDA_TRY(call)                                           \

@@ -10,6 +10,12 @@ int apply_f64(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
               const double *p, double *y, const uint8_t *mask, cudaStream_t st);
 int filter_launch(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, int mode, const float *hs,
                   const float *in, const uint8_t *preserved, float *out, cudaStream_t st);
+// FP64 apply through the modal element form: an element pass writes the 24 corner
+// contributions of every element to C (24 * n_elem doubles), a node pass sums them in a
+// fixed order. Requires ctx->modal_ok.
+size_t apply_f64_modal_ws_bytes(int nx, int ny, int nz);
+int apply_f64_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
+                    const double *p, double *y, const uint8_t *mask, double *C, cudaStream_t st);
 // A 4 KiB pinned host buffer private to the calling thread (for small status reads).
 void *thread_pinned();
 }  // namespace gbs

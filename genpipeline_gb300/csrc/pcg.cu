@@ -12,9 +12,12 @@
 #include <string.h>
 
 #include <chrono>
+#include <mutex>
+#include <string>
+#include <unordered_map>
 #include <vector>
 
-#include "apply_tile.cuh"
+#include "apply_modal.cuh"
 #include "internal.h"
 
 namespace gbs {
@@ -123,8 +126,10 @@ __device__ bool last_block3(double a, double b, double c, double *partials, unsi
 // r = D b - q (q = D K D x0), x0 fixed entries zeroed, p_{-1} = 0; sums r.z, r.r, (Db).(Db).
 __global__ void pcg_init_kernel(int64_t nd, const float *__restrict__ b, const float *__restrict__ q,
                                 const uint8_t *__restrict__ mask, const float *__restrict__ dinv, float *r, float *pprev,
-                                float *xu, double *partials, PcgScalars *sc, double tol, int max_iter) {
-    double rz = 0.0, rr = 0.0, bb = 0.0;
+                                float *xu, double *partials, PcgScalars *sc, double tol, int max_iter,
+                                int max_trips) {
+    // per-thread partials in FP32 (a few terms each), block and grid sums in FP64
+    float rz = 0.0f, rr = 0.0f, bb = 0.0f;
     for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
         const bool fx = dof_fixed(mask, d);
         const float bd = fx ? 0.0f : b[d];
@@ -132,9 +137,9 @@ __global__ void pcg_init_kernel(int64_t nd, const float *__restrict__ b, const f
         r[d] = rd;
         pprev[d] = 0.0f;
         if (fx) xu[d] = 0.0f;
-        rz += (double)rd * (double)rd * (double)dinv[d];
-        rr += (double)rd * (double)rd;
-        bb += (double)bd * (double)bd;
+        rz = fmaf(rd * dinv[d], rd, rz);
+        rr = fmaf(rd, rd, rr);
+        bb = fmaf(bd, bd, bb);
     }
     __shared__ double tot[3];
     if (last_block3(rz, rr, bb, partials, &sc->counter, tot) && threadIdx.x == 0) {
@@ -147,6 +152,8 @@ __global__ void pcg_init_kernel(int64_t nd, const float *__restrict__ b, const f
         sc->pap = 0.0;
         sc->iter = 0;
         sc->max_iter = max_iter;
+        sc->trips = 0;
+        sc->max_trips = max_trips;
         sc->status = GBS_OK;
         const bool fin = isfinite(tot[0]) && isfinite(tot[1]) && isfinite(tot[2]);
         sc->done = (!fin || sc->bnorm == 0.0 || sqrt(tot[1]) < tol * sc->bnorm || max_iter <= 0) ? 1 : 0;
@@ -161,12 +168,12 @@ __global__ void __launch_bounds__(256) pcg_update_kernel(int64_t nd, const float
     if (sc->done) return;
     const int it = sc->iter;
     const float alpha = (float)sc->alpha[it & 1];
-    double rz = 0.0, rr = 0.0;
+    float rz = 0.0f, rr = 0.0f;  // per-thread FP32 partials, FP64 block and grid sums
     for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
         const float rd = fmaf(-alpha, ap[d], r[d]);
         r[d] = rd;
-        rr += (double)rd * (double)rd;
-        rz += (double)rd * (double)rd * (double)dinv[d];
+        rr = fmaf(rd, rd, rr);
+        rz = fmaf(rd * dinv[d], rd, rz);
     }
     __shared__ double tot[3];
     if (last_block3(rz, rr, 0.0, partials, &sc->counter, tot) && threadIdx.x == 0) {
@@ -211,14 +218,19 @@ static int read_scalars(const PcgScalars *d, PcgScalars *h, cudaStream_t st) {
 // Launches one K1+K2 iteration.
 static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
                          const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st, cudaEvent_t after_k1) {
-    TileArgs<float> A{nx, ny, nz, x, nullptr, w.ap, mask};
     PcgArgs pa{w.r, w.dinv, w.p0, w.p1, u, w.partials, w.sc};
-    const dim3 g = tile_grid<TileF>(nx, ny, nz), b = tile_block<TileF>();
-    if (ctx->translation_free)
-        apply_tile_kernel<float, KeF, TileF::X, TileF::Y, TileF::Z, true, MODE_PCG><<<g, b, 0, st>>>(A, law, ctx->kef, pa);
-    else
-        apply_tile_kernel<float, KeF, TileF::X, TileF::Y, TileF::Z, false, MODE_PCG><<<g, b, 0, st>>>(A, law, ctx->kef, pa);
-    GBS_LAUNCH_CHECK("apply_tile_kernel<PCG>");
+    if (ctx->modal_ok && modal_fits(nz)) {
+        int rc = launch_modal<MODE_PCG>(ctx, nx, ny, nz, law, x, nullptr, w.ap, mask, pa, st);
+        if (rc) return rc;
+    } else {
+        TileArgs<float> A{nx, ny, nz, x, nullptr, w.ap, mask};
+        const dim3 g = tile_grid<TileF>(nx, ny, nz), b = tile_block<TileF>();
+        if (ctx->translation_free)
+            apply_tile_kernel<float, KeF, TileF::X, TileF::Y, TileF::Z, true, MODE_PCG><<<g, b, 0, st>>>(A, law, ctx->kef, pa);
+        else
+            apply_tile_kernel<float, KeF, TileF::X, TileF::Y, TileF::Z, false, MODE_PCG><<<g, b, 0, st>>>(A, law, ctx->kef, pa);
+        GBS_LAUNCH_CHECK("apply_tile_kernel<PCG>");
+    }
     if (after_k1) GBS_CUDA_TRY(cudaEventRecord(after_k1, st));
     const int64_t nd = n_dof_of(nx, ny, nz);
     pcg_update_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.ap, w.dinv, w.r, w.partials, w.sc);
@@ -227,6 +239,147 @@ static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const La
 }
 
 // FP32 PCG. u: x0 in, solution out. Returns GBS_OK and fills *out (status inside).
+// ---- device-driven PCG loop: one CUDA graph with a WHILE node ------------------------------
+// Body: kLoopUnroll x (K1, K2) and a one-thread kernel that sets the loop condition from
+// the device flag `done`. K1/K2 return at once when done is set, so a finished solve costs
+// at most kLoopUnroll-1 empty iterations. The condition kernel also counts trips and stops
+// the loop with GBS_ETIMEOUT after max_trips (set from max_iter), so the loop always ends.
+constexpr int kLoopUnroll = 8;
+
+__global__ void pcg_loop_cond_kernel(cudaGraphConditionalHandle h, PcgScalars *sc) {
+    const int trips = sc->trips + 1;
+    sc->trips = trips;
+    bool stop = sc->done != 0;
+    if (!stop && trips >= sc->max_trips) {
+        sc->done = 1;
+        sc->status = GBS_ETIMEOUT;
+        stop = true;
+    }
+    cudaGraphSetConditional(h, stop ? 0u : 1u);
+}
+
+struct GraphCache {
+    std::mutex mu;
+    std::unordered_map<std::string, cudaGraphExec_t> map;
+    cudaStream_t cap = nullptr;  // private capture stream
+};
+
+void *graph_cache_create() { return new GraphCache(); }
+
+void graph_cache_destroy(void *p) {
+    GraphCache *gc = (GraphCache *)p;
+    if (!gc) return;
+    for (auto &kv : gc->map)
+        if (kv.second) cudaGraphExecDestroy(kv.second);
+    if (gc->cap) cudaStreamDestroy(gc->cap);
+    delete gc;
+}
+
+struct LoopKey {
+    const void *ws, *x, *mask, *u;
+    int nx, ny, nz, kind;
+    float penal, e0, emin, xmin;
+    unsigned ke_version;
+    int modal;
+};
+
+static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
+                         const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st, cudaEvent_t after_k1);
+
+// Builds (or finds) the instantiated loop graph for this problem and buffer set.
+static int loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
+                      const uint8_t *mask, float *u, const PcgWs &w, cudaGraphExec_t *out) {
+    GraphCache *gc = (GraphCache *)ctx->graphs;
+    if (!gc) return set_error(GBS_ECUDA, "no graph cache");
+    const bool modal = ctx->modal_ok && modal_fits(nz);
+    LoopKey k;
+    memset(&k, 0, sizeof k);
+    k.ws = w.sc;
+    k.x = x;
+    k.mask = mask;
+    k.u = u;
+    k.nx = nx;
+    k.ny = ny;
+    k.nz = nz;
+    k.kind = law.kind;
+    k.penal = law.penal;
+    k.e0 = law.e0;
+    k.emin = law.emin;
+    k.xmin = law.xmin;
+    k.ke_version = ctx->ke_version;
+    k.modal = modal ? 1 : 0;
+    const std::string key((const char *)&k, sizeof k);
+    std::lock_guard<std::mutex> lock(gc->mu);
+    auto it = gc->map.find(key);
+    if (it != gc->map.end()) {
+        *out = it->second;
+        return GBS_OK;
+    }
+    if (gc->map.size() >= 64) {
+        for (auto &kv : gc->map) cudaGraphExecDestroy(kv.second);
+        gc->map.clear();
+    }
+    if (modal) {
+        const int r = modal_prepare<MODE_PCG>(ctx, nz);
+        if (r < 0) return -r;
+    }
+    if (!gc->cap) GBS_CUDA_TRY(cudaStreamCreateWithFlags(&gc->cap, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    GBS_CUDA_TRY(cudaGraphCreate(&g, 0));
+    int rc = GBS_OK;
+    cudaGraphExec_t exec = nullptr;
+    do {
+        cudaGraphConditionalHandle h;
+        cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+        if (e != cudaSuccess) {
+            rc = cuda_error(e, "cudaGraphConditionalHandleCreate");
+            break;
+        }
+        // cudaGraphNodeParams has a union with non-trivial members: zero-initialised storage.
+        alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)] = {};
+        cudaGraphNodeParams &cp = *reinterpret_cast<cudaGraphNodeParams *>(cp_buf);
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+        if (e != cudaSuccess) {
+            rc = cuda_error(e, "cudaGraphAddNode(while)");
+            break;
+        }
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(gc->cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            rc = cuda_error(e, "cudaStreamBeginCaptureToGraph");
+            break;
+        }
+        set_capturing(true);
+        for (int i = 0; i < kLoopUnroll && rc == GBS_OK; ++i)
+            rc = pcg_iteration(ctx, nx, ny, nz, law, x, mask, u, w, gc->cap, nullptr);
+        if (rc == GBS_OK) {
+            pcg_loop_cond_kernel<<<1, 1, 0, gc->cap>>>(h, w.sc);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) rc = cuda_error(e, "pcg_loop_cond_kernel");
+        }
+        set_capturing(false);
+        cudaGraph_t captured = nullptr;
+        e = cudaStreamEndCapture(gc->cap, &captured);
+        if (rc == GBS_OK && e != cudaSuccess) rc = cuda_error(e, "cudaStreamEndCapture");
+        if (rc != GBS_OK) break;
+        e = cudaGraphInstantiate(&exec, g, 0);
+        if (e != cudaSuccess) {
+            rc = cuda_error(e, "cudaGraphInstantiate");
+            exec = nullptr;
+        }
+    } while (0);
+    cudaGraphDestroy(g);
+    if (rc != GBS_OK) return rc;
+    gc->map.emplace(key, exec);
+    *out = exec;
+    return GBS_OK;
+}
+
 // Optional profiling (prof != nullptr): CUDA events around every K1 launch; only the
 // launches of iterations that actually ran (the device counter advanced) are summed.
 struct ApplyProfile {
@@ -246,11 +399,25 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
     int rc = apply_f32(ctx, nx, ny, nz, glaw, x, u, w.ap, mask, st);
     if (rc) return rc;
     pcg_init_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, b, w.ap, mask, w.dinv, w.r, w.p1, u, w.partials, w.sc, rtol,
-                                                        max_iter);
+                                                        max_iter, (max_iter + kLoopUnroll - 1) / kLoopUnroll + 2);
     GBS_LAUNCH_CHECK("pcg_init_kernel");
     PcgScalars h;
     rc = read_scalars(w.sc, &h, st);
     if (rc) return rc;
+    if (!prof && !h.done) {
+        cudaGraphExec_t exec = nullptr;
+        if (loop_graph(ctx, nx, ny, nz, law, x, mask, u, w, &exec) == GBS_OK) {
+            GBS_CUDA_TRY(cudaGraphLaunch(exec, st));
+            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc);
+            GBS_LAUNCH_CHECK("pcg_finalize_kernel");
+            rc = read_scalars(w.sc, &h, st);
+            if (rc) return rc;
+            count_launches(h.trips * (2 * kLoopUnroll + 1));
+            *out = h;
+            return GBS_OK;
+        }
+        // graph construction failed: fall through to host-launched iterations
+    }
     int chunk = check_every > 0 ? check_every : 16;
     const int max_chunk = check_every > 0 ? check_every : 128;
     std::vector<cudaEvent_t> ev;
@@ -306,12 +473,13 @@ struct SolveWs {
     float *b32, *d32;
     double *partials;
     void *pcg;
+    double *elem;  // 24 * n_elem doubles for the modal FP64 residual
 };
 
 static size_t solve_ws_bytes_impl(int nx, int ny, int nz) {
     const size_t nd = (size_t)n_dof_of(nx, ny, nz);
     return al256(sizeof(OuterScalars)) + al256(nd * 8) + 2 * al256(nd * 4) + al256(3 * 4096 * 8) +
-           pcg_ws_bytes_impl(nx, ny, nz);
+           pcg_ws_bytes_impl(nx, ny, nz) + al256(apply_f64_modal_ws_bytes(nx, ny, nz));
 }
 
 static SolveWs solve_ws(void *ws, int nx, int ny, int nz) {
@@ -329,6 +497,8 @@ static SolveWs solve_ws(void *ws, int nx, int ny, int nz) {
     w.partials = (double *)p;
     p += al256(3 * 4096 * 8);
     w.pcg = p;
+    p += pcg_ws_bytes_impl(nx, ny, nz);
+    w.elem = (double *)p;
     return w;
 }
 
@@ -390,7 +560,8 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
     const int max_outer = o->max_outer > 0 ? o->max_outer : 20;
     const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-3;
     for (;;) {
-        int rc = apply_f64(ctx, nx, ny, nz, law, x, u, w.r64, mask, st);
+        int rc = ctx->modal_ok ? apply_f64_modal(ctx, nx, ny, nz, law, x, u, w.r64, mask, w.elem, st)
+                               : apply_f64(ctx, nx, ny, nz, law, x, u, w.r64, mask, st);
         if (rc) return rc;
         // resid64 reads q from r64 and overwrites it in place (element-wise, same index).
         resid64_kernel<<<vb, 256, 0, st>>>(nd, f, w.r64, mask, w.r64, w.partials, w.os);
@@ -596,15 +767,101 @@ static CsrWs csr_ws(void *ws, int64_t n) {
 
 using namespace gbs;
 
+static bool grid_ok(int nx, int ny, int nz) {
+    return nx > 0 && ny > 0 && nz > 0 && (int64_t)(nx + 1) * (ny + 1) * (nz + 1) < (1LL << 31) / 3;
+}
+
 extern "C" size_t gbsimp_pcg_ws_bytes(int nx, int ny, int nz) { return pcg_ws_bytes_impl(nx, ny, nz); }
+
+extern "C" size_t gbsimp_time_pcg_apply_ws_bytes(int nx, int ny, int nz) {
+    return pcg_ws_bytes_impl(nx, ny, nz) + al256((size_t)n_dof_of(nx, ny, nz) * sizeof(float));
+}
+
+__global__ void fill_f32_kernel(int64_t n, float v, float *a) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
+}
+
+extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x,
+                                     const uint8_t *node_mask, int reps, void *ws, size_t ws_bytes,
+                                     double *seconds_per_launch, void *stream) {
+    if (!ctx || !glaw || !x || !ws || !seconds_per_launch || reps <= 0 || reps > 100000 || !grid_ok(nx, ny, nz))
+        return set_error(GBS_EINVAL, "gbsimp_time_pcg_apply: bad arguments");
+    if (ws_bytes < gbsimp_time_pcg_apply_ws_bytes(nx, ny, nz))
+        return set_error(GBS_EINVAL, "gbsimp_time_pcg_apply: workspace too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t nd = n_dof_of(nx, ny, nz);
+    PcgWs w = pcg_ws(ws, nx, ny, nz);
+    float *xu = (float *)((char *)ws + pcg_ws_bytes_impl(nx, ny, nz));
+    const Law<float> law = make_law<float>(*glaw);
+    // A state on which every K1 launch does full work: r = 1 (p = r/diag > 0 on free DOFs,
+    // so p.Ap > 0), beta = 0, iteration 0 (K2 never runs, so every launch repeats step 0).
+    GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
+    dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, law, ctx->kef, x, node_mask, w.dinv);
+    fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 1.0f, w.r);
+    fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.p1);
+    fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, xu);
+    GBS_LAUNCH_CHECK("time_pcg_apply setup");
+    const bool modal = ctx->modal_ok && modal_fits(nz);
+    if (modal) {
+        const int r = modal_prepare<MODE_PCG>(ctx, nz);
+        if (r < 0) return -r;
+    }
+    GraphCache *gc = (GraphCache *)ctx->graphs;
+    std::lock_guard<std::mutex> lock(gc->mu);
+    if (!gc->cap) GBS_CUDA_TRY(cudaStreamCreateWithFlags(&gc->cap, cudaStreamNonBlocking));
+    GBS_CUDA_TRY(cudaStreamBeginCapture(gc->cap, cudaStreamCaptureModeThreadLocal));
+    set_capturing(true);
+    int rc = GBS_OK;
+    PcgArgs pa{w.r, w.dinv, w.p0, w.p1, xu, w.partials, w.sc};
+    for (int i = 0; i < reps && rc == GBS_OK; ++i) {
+        if (modal) {
+            rc = launch_modal<MODE_PCG>(ctx, nx, ny, nz, law, x, nullptr, w.ap, node_mask, pa, gc->cap);
+        } else {
+            TileArgs<float> A{nx, ny, nz, x, nullptr, w.ap, node_mask};
+            const dim3 g = tile_grid<TileF>(nx, ny, nz), b = tile_block<TileF>();
+            if (ctx->translation_free)
+                apply_tile_kernel<float, KeF, TileF::X, TileF::Y, TileF::Z, true, MODE_PCG><<<g, b, 0, gc->cap>>>(A, law, ctx->kef, pa);
+            else
+                apply_tile_kernel<float, KeF, TileF::X, TileF::Y, TileF::Z, false, MODE_PCG><<<g, b, 0, gc->cap>>>(A, law, ctx->kef, pa);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) rc = cuda_error(e, "apply_tile_kernel<PCG>");
+        }
+    }
+    set_capturing(false);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(gc->cap, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_error(e, "cudaStreamEndCapture");
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGraphInstantiate");
+    cudaEvent_t e0, e1;
+    GBS_CUDA_TRY(cudaEventCreate(&e0));
+    GBS_CUDA_TRY(cudaEventCreate(&e1));
+    rc = GBS_OK;
+    float ms = 0.0f;
+    if ((e = cudaGraphLaunch(exec, st)) != cudaSuccess ||       // warm-up replay
+        (e = cudaEventRecord(e0, st)) != cudaSuccess || (e = cudaGraphLaunch(exec, st)) != cudaSuccess ||
+        (e = cudaEventRecord(e1, st)) != cudaSuccess || (e = cudaEventSynchronize(e1)) != cudaSuccess ||
+        (e = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess)
+        rc = cuda_error(e, "time_pcg_apply replay");
+    count_launches(2 * reps);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaGraphExecDestroy(exec);
+    if (rc) return rc;
+    *seconds_per_launch = 1e-3 * ms / reps;
+    return GBS_OK;
+}
 
 extern "C" size_t gbsimp_solve_ws_bytes(int nx, int ny, int nz) { return solve_ws_bytes_impl(nx, ny, nz); }
 
 extern "C" size_t gbsimp_pcg_csr_ws_bytes(int64_t n) { return csr_ws_bytes_impl(n); }
 
-static bool grid_ok(int nx, int ny, int nz) {
-    return nx > 0 && ny > 0 && nz > 0 && (int64_t)(nx + 1) * (ny + 1) * (nz + 1) < (1LL << 31) / 3;
-}
 
 extern "C" int gbsimp_pcg_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
                               const float *b, const uint8_t *node_mask, float *u, const gbsimp_solve_opts *opts,

@@ -87,6 +87,11 @@ class Engine:
         L.check(L.load().gbsimp_ke_quadrature(float(nu), float(e0), k.ctypes.data_as(C.POINTER(C.c_double))))
         return k.reshape(24, 24)
 
+    def apply_path(self, nz: int) -> str:
+        """'modal' or 'dense': the FP32 apply kernel this context uses for z extent nz."""
+        r = self.lib.gbsimp_apply_path(self.ctx, int(nz))
+        return {1: "modal", 0: "dense"}[r]
+
     # ---- workspaces ---------------------------------------------------------------------
     def workspace(self, key: str, nbytes: int) -> torch.Tensor:
         """Grow-only scratch buffer per (host thread, purpose): threads that share an engine
@@ -222,6 +227,18 @@ class Engine:
         L.check(self.lib.gbsimp_pcg_f32(self.ctx, nx, ny, nz, C.byref(law), _p(x), _p(b), _p(mask), _p(u), C.byref(o),
                                         C.byref(st), _p(ws), nb, _stream()))
         return st.as_dict()
+
+    def time_pcg_apply(self, grid: Grid, law: L.Law, x: torch.Tensor, mask: Optional[torch.Tensor] = None,
+                       reps: int = 50) -> float:
+        """Mean device seconds per launch of the fused PCG apply kernel on densities x."""
+        nx, ny, nz = grid
+        _need(x, torch.float32, n_elem(grid), "x")
+        nb = self.lib.gbsimp_time_pcg_apply_ws_bytes(nx, ny, nz)
+        ws = self.workspace("time_apply", nb)
+        sec = C.c_double()
+        L.check(self.lib.gbsimp_time_pcg_apply(self.ctx, nx, ny, nz, C.byref(law), _p(x), _p(mask), int(reps), _p(ws),
+                                               nb, C.byref(sec), _stream()))
+        return sec.value
 
     def solve(self, grid: Grid, law: L.Law, x: torch.Tensor, f: torch.Tensor, mask: Optional[torch.Tensor],
               u: torch.Tensor, rtol=1e-8, inner_rtol=1e-3, max_iter=100000, max_outer=30, check_every=0,

@@ -113,6 +113,10 @@ int gbsimp_get_ke(const gbsimp_ctx *ctx, double *ke576);
 int gbsimp_apply_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
                      const float *x, const float *p, float *y, const uint8_t *node_mask,
                      void *stream);
+/* Which FP32 kernel serves gbsimp_apply_f32 / the PCG for this context and z extent:
+ * 1 = modal (Hadamard) element kernel, used when Ke has the structure of an isotropic cube
+ * element and nz <= 446; 0 = dense 24x24 node-gather kernel (any Ke); -1 = bad context. */
+int gbsimp_apply_path(const gbsimp_ctx *ctx, int nz);
 int gbsimp_apply_f64(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
                      const float *x, const double *p, double *y, const uint8_t *node_mask,
                      void *stream);
@@ -168,13 +172,25 @@ int gbsimp_oc_result(gbsimp_ctx *ctx, const void *ws, double *lambda_out, int *s
 /* ---- linear solves ----------------------------------------------------------------- */
 /* FP32 Jacobi-PCG on the free DOFs (simp_solver_gpu.py:328-379, _solve :571-705):
  * u holds x0 on entry (fixed DOFs are zeroed), the solution on exit. The stop test is
- * ||r|| < rtol ||D b||, checked on the device every iteration; the host reads the
- * status every opts->check_every iterations (the call synchronises the stream). */
+ * ||r|| < rtol ||D b||, checked on the device every iteration. The iteration loop runs on
+ * the device: a CUDA graph (cached per buffer set) whose WHILE node repeats 8 iterations
+ * while the device-side stop flag is clear, with a hard cap derived from max_iter
+ * (GBS_ETIMEOUT). With opts->profile the host launches the iterations instead, checking
+ * every opts->check_every iterations, and times each apply launch. Synchronises the stream. */
 size_t gbsimp_pcg_ws_bytes(int nx, int ny, int nz);
 int gbsimp_pcg_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
                    const float *x, const float *b, const uint8_t *node_mask, float *u,
                    const gbsimp_solve_opts *opts, gbsimp_solve_stats *stats, void *ws,
                    size_t ws_bytes, void *stream);
+/* Measures the fused PCG apply kernel (the apply that also forms p = z + beta p, updates
+ * the iterate and reduces p.Ap -- the kernel that dominates gbsimp_pcg_f32 and
+ * gbsimp_solve) on the densities x: reps back-to-back launches replayed from one CUDA graph
+ * and timed with CUDA events on the stream. Writes the mean device time per launch.
+ * Synchronises the stream. */
+size_t gbsimp_time_pcg_apply_ws_bytes(int nx, int ny, int nz);
+int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
+                          const float *x, const uint8_t *node_mask, int reps, void *ws,
+                          size_t ws_bytes, double *seconds_per_launch, void *stream);
 /* FP32 PCG inner solves with FP64 outer defect correction: r = D(f - K u) in FP64, FP32
  * PCG on K d = r to inner_rtol, u += d, until ||r|| <= rtol ||D f||. u (FP64) holds the
  * warm start on entry. Synchronises the stream. */

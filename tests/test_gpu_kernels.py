@@ -66,6 +66,48 @@ def test_apply_vs_oracle(eng, grid, law, masked):
     np.testing.assert_allclose(y32, ref, rtol=0, atol=2e-6 * np.abs(ref).max())
 
 
+def _perturbed_ke():
+    """SPD quadrature Ke plus a tiny symmetric term outside the modal pattern: it forces the
+    dense kernel while staying numerically the same operator to ~1e-10."""
+    ke = O.ke_quadrature()
+    d = np.zeros((24, 24))
+    d[0, 9] = d[9, 0] = 1e-10
+    return ke + d
+
+
+@pytest.mark.parametrize("grid", [(1, 1, 1), (33, 7, 5), (17, 9, 37), (40, 64, 64), (3, 2, 450)])
+@pytest.mark.parametrize("masked", [False, True])
+def test_modal_and_dense_kernels_agree(eng, grid, masked):
+    nx, ny, nz = grid
+    dense = Engine(ke=_perturbed_ke())
+    assert dense.apply_path(nz) == "dense"
+    assert eng.apply_path(nz) == ("modal" if nz <= 446 else "dense")
+    x, p = _rand(grid, 21)
+    fixed = bcs.reference_cpu(*grid, {"fixed_face": ["x_min", "y_max"]})[1] if masked else None
+    m = _cuda(bcs.node_mask(*grid, fixed)) if masked else None
+    lw = L.make_law("modified", 3.0)
+    ym = eng.apply(grid, lw, _cuda(x), _cuda(p, torch.float32), m).cpu().numpy()
+    yd = dense.apply(grid, lw, _cuda(x), _cuda(p, torch.float32), m).cpu().numpy()
+    ref = O.apply(grid, O.ke_quadrature(), O.moduli(x.astype(np.float64), _mat("modified")), p,
+                  bcs.dof_mask(*grid, fixed) if masked else None)
+    np.testing.assert_allclose(ym, ref, rtol=0, atol=2e-6 * np.abs(ref).max())
+    np.testing.assert_allclose(yd, ref, rtol=0, atol=2e-6 * np.abs(ref).max())
+
+
+def test_pcg_dense_path_matches_modal_path(eng):
+    grid = (20, 10, 14)
+    f, fixed, x = _problem(grid)
+    m = _cuda(bcs.node_mask(*grid, fixed))
+    lw = L.make_law("modified", 3.0)
+    out = []
+    for e in (eng, Engine(ke=_perturbed_ke())):
+        u = torch.zeros(n_dof(grid), dtype=torch.float64, device="cuda")
+        st = e.solve(grid, lw, _cuda(x), _cuda(f), m, u, rtol=1e-8)
+        assert st["status"] == L.GBS_OK
+        out.append(u.cpu().numpy())
+    np.testing.assert_allclose(out[0], out[1], rtol=0, atol=1e-6 * np.abs(out[1]).max())
+
+
 @pytest.mark.parametrize("grid", [(5, 4, 3), (17, 9, 37)])
 def test_apply_literal_reference_ke(grid, ke_lit):
     """Non-symmetric, translation-carrying reference table: the non-subtracting kernel."""
@@ -193,6 +235,7 @@ def test_oc_large_vs_oracle(eng):
 
 
 def _problem(grid, case="cantilever", law="modified", seed=0):
+    """Load case and seeded random densities in [0.05, 1)."""
     f, fixed = bcs.LOAD_CASES[case](*grid)
     rng = np.random.default_rng(seed)
     x = rng.uniform(0.05, 1.0, np.prod(grid)).astype(np.float32)
@@ -229,6 +272,32 @@ def test_solve_refined_vs_oracle(eng, grid, case, law):
     c_ref = float(f @ uref)
     assert float(f @ ug) == pytest.approx(c_ref, rel=1e-6)
     np.testing.assert_allclose(ug, uref, rtol=0, atol=1e-5 * np.abs(uref).max())
+
+
+def test_device_loop_and_host_loop_agree_bitwise(eng):
+    """The graph WHILE loop and the host-launched (profiled) loop run the same kernels in the
+    same order: identical bits, identical iteration counts."""
+    grid = (24, 12, 12)
+    f, fixed, x = _problem(grid, "top_patch")
+    m = _cuda(bcs.node_mask(*grid, fixed))
+    lw = L.make_law("modified", 3.0)
+    res = []
+    for prof in (False, True, False):
+        u = torch.zeros(n_dof(grid), dtype=torch.float64, device="cuda")
+        st = eng.solve(grid, lw, _cuda(x), _cuda(f), m, u, rtol=1e-8, profile=prof)
+        assert st["status"] == L.GBS_OK
+        res.append((u.cpu().numpy(), st["iterations"]))
+        if prof:
+            assert st["apply_launches"] == st["iterations"] and st["apply_seconds"] > 0
+    assert res[0][1] == res[1][1] == res[2][1]
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][0], res[2][0])
+
+
+def test_time_pcg_apply(eng):
+    grid = (32, 16, 16)
+    f, fixed, x = _problem(grid)
+    sec = eng.time_pcg_apply(grid, L.make_law("modified", 3.0), _cuda(x), _cuda(bcs.node_mask(*grid, fixed)), reps=10)
+    assert 0 < sec < 1e-2
 
 
 def test_solve_warm_start_and_zero_load(eng):
