@@ -458,12 +458,13 @@ extern "C" int gbsimp_filter(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmi
 
 extern "C" size_t gbsimp_oc_ws_bytes(int nx, int ny, int nz) { return oc_ws_bytes((int64_t)nx * ny * nz); }
 
-extern "C" int gbsimp_oc_prepare(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const uint8_t *preserved,
-                                 void *ws, size_t ws_bytes, void *stream) {
-    if (!ctx || nx <= 0 || ny <= 0 || nz <= 0 || !ws) return set_error(GBS_EINVAL, "gbsimp_oc_prepare: bad arguments");
+namespace gbs {
+
+size_t oc_ws_bytes_impl(int64_t n) { return oc_ws_bytes(n); }
+
+int oc_prepare_impl(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const uint8_t *preserved, void *ws,
+                    cudaStream_t st) {
     const int64_t n = (int64_t)nx * ny * nz;
-    if (ws_bytes < oc_ws_bytes(n)) return set_error(GBS_EINVAL, "gbsimp_oc_prepare: workspace too small");
-    cudaStream_t st = (cudaStream_t)stream;
     OcWs w = oc_ws(ws, n);
     GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(OcScalars), st));
     int rc = filter_launch(ctx, nx, ny, nz, rmin, 2, nullptr, nullptr, nullptr, w.hs, st);
@@ -476,16 +477,9 @@ extern "C" int gbsimp_oc_prepare(gbsimp_ctx *ctx, int nx, int ny, int nz, double
     return GBS_OK;
 }
 
-extern "C" int gbsimp_oc(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const gbsimp_oc_params *prm,
-                         const float *x, const float *dc, const uint8_t *preserved, float *xnew, float *xphys,
-                         void *ws, size_t ws_bytes, void *stream) {
-    if (!ctx || !prm || !x || !dc || !xnew || !xphys || !ws || nx <= 0 || ny <= 0 || nz <= 0)
-        return set_error(GBS_EINVAL, "gbsimp_oc: bad arguments");
+int oc_run_impl(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const gbsimp_oc_params *prm, const float *x,
+                const float *dc, const uint8_t *preserved, float *xnew, float *xphys, void *ws, cudaStream_t st) {
     const int64_t n = (int64_t)nx * ny * nz;
-    if (ws_bytes < oc_ws_bytes(n)) return set_error(GBS_EINVAL, "gbsimp_oc: workspace too small");
-    if (prm->max_bisect <= 0 || prm->max_bisect > 1000) return set_error(GBS_EINVAL, "gbsimp_oc: max_bisect out of range");
-    if (x == xnew) return set_error(GBS_EINVAL, "gbsimp_oc: x and xnew must not alias");
-    cudaStream_t st = (cudaStream_t)stream;
     OcWs w = oc_ws(ws, n);
     OcParams P;
     P.move = (float)prm->move;
@@ -506,6 +500,34 @@ extern "C" int gbsimp_oc(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, c
     oc_final_kernel<<<elem_blocks(ctx, n, 256), 256, 0, st>>>(n, P, x, dc, preserved, w.sc, xnew);
     GBS_LAUNCH_CHECK("oc_final_kernel");
     return filter_launch(ctx, nx, ny, nz, rmin, 0, w.hs, xnew, preserved, xphys, st);
+}
+
+int oc_check_args(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_oc_params *prm, const float *x,
+                  const float *dc, const float *xnew, const float *xphys) {
+    if (!ctx || !prm || !x || !dc || !xnew || !xphys || nx <= 0 || ny <= 0 || nz <= 0)
+        return set_error(GBS_EINVAL, "gbsimp_oc: bad arguments");
+    if (prm->max_bisect <= 0 || prm->max_bisect > 1000)
+        return set_error(GBS_EINVAL, "gbsimp_oc: max_bisect out of range");
+    if (x == xnew) return set_error(GBS_EINVAL, "gbsimp_oc: x and xnew must not alias");
+    return GBS_OK;
+}
+
+}  // namespace gbs
+
+extern "C" int gbsimp_oc_prepare(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const uint8_t *preserved,
+                                 void *ws, size_t ws_bytes, void *stream) {
+    if (!ctx || nx <= 0 || ny <= 0 || nz <= 0 || !ws) return set_error(GBS_EINVAL, "gbsimp_oc_prepare: bad arguments");
+    if (ws_bytes < oc_ws_bytes((int64_t)nx * ny * nz)) return set_error(GBS_EINVAL, "gbsimp_oc_prepare: workspace too small");
+    return oc_prepare_impl(ctx, nx, ny, nz, rmin, preserved, ws, (cudaStream_t)stream);
+}
+
+extern "C" int gbsimp_oc(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const gbsimp_oc_params *prm,
+                         const float *x, const float *dc, const uint8_t *preserved, float *xnew, float *xphys,
+                         void *ws, size_t ws_bytes, void *stream) {
+    int rc = oc_check_args(ctx, nx, ny, nz, prm, x, dc, xnew, xphys);
+    if (rc) return rc;
+    if (!ws || ws_bytes < oc_ws_bytes((int64_t)nx * ny * nz)) return set_error(GBS_EINVAL, "gbsimp_oc: workspace too small");
+    return oc_run_impl(ctx, nx, ny, nz, rmin, prm, x, dc, preserved, xnew, xphys, ws, (cudaStream_t)stream);
 }
 
 extern "C" int gbsimp_oc_result(gbsimp_ctx *ctx, const void *ws, double *lambda_out, int *steps_out, void *stream) {

@@ -16,6 +16,14 @@ int filter_launch(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, in
 size_t apply_f64_modal_ws_bytes(int nx, int ny, int nz);
 int apply_f64_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
                     const double *p, double *y, const uint8_t *mask, double *C, cudaStream_t st);
+// OC update with an explicit scratch pointer (layout of gbsimp_oc_ws_bytes).
+size_t oc_ws_bytes_impl(int64_t n_elem);
+int oc_check_args(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_oc_params *prm, const float *x,
+                  const float *dc, const float *xnew, const float *xphys);
+int oc_prepare_impl(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const uint8_t *preserved, void *ws,
+                    cudaStream_t st);
+int oc_run_impl(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const gbsimp_oc_params *prm, const float *x,
+                const float *dc, const uint8_t *preserved, float *xnew, float *xphys, void *ws, cudaStream_t st);
 // A 4 KiB pinned host buffer private to the calling thread (for small status reads).
 void *thread_pinned();
 }  // namespace gbs
