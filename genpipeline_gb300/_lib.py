@@ -95,6 +95,7 @@ SIGNATURES = {
     "gbsimp_oc_ws_bytes": (_SZ, [_I, _I, _I]),
     "gbsimp_oc_prepare": (_I, [_P, _I, _I, _I, _D, _P, _P, _SZ, _P]),
     "gbsimp_oc": (_I, [_P, _I, _I, _I, _D, C.POINTER(OcParams), _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "gbsimp_oc_noalloc": (_I, [_P, _I, _I, _I, _D, C.POINTER(OcParams), _P, _P, _P, _P, _P, _P]),
     "gbsimp_oc_result": (_I, [_P, _P, C.POINTER(_D), C.POINTER(_I), _P]),
     "gbsimp_pcg_ws_bytes": (_SZ, [_I, _I, _I]),
     "gbsimp_pcg_f32": (_I, [_P, _I, _I, _I, C.POINTER(Law), _P, _P, _P, _P, C.POINTER(SolveOpts),

@@ -165,6 +165,21 @@ int gbsimp_oc(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin,
               const gbsimp_oc_params *prm, const float *x, const float *dc,
               const uint8_t *preserved, float *xnew, float *xphys, void *ws, size_t ws_bytes,
               void *stream);
+/* OC update that allocates nothing (no counterpart in the reference). It exists for callers
+ * that cannot allocate device memory: a host-language plugin that reaches the GPU only
+ * through this C ABI and has no CUDA allocator of its own, or a serving process whose device
+ * memory is reserved up front and must not grow per request. Same inputs, outputs and
+ * results as gbsimp_oc, but the scratch is a fixed 16.1 MiB device array inside the library
+ * (held on every GPU that loads the library until the process exits), so grids above
+ * GBSIMP_OC_NOALLOC_MAX_ELEMENTS elements are rejected with GBS_EINVAL. The first call on a
+ * device looks up that array's device address (call it with the context's device current);
+ * make that first call before any stream capture. All calls share the one array and each
+ * call re-initialises what it reads: calls that overlap on the GPU (other streams, other
+ * threads) race and must not be issued. */
+#define GBSIMP_OC_NOALLOC_MAX_ELEMENTS 2097152
+int gbsimp_oc_noalloc(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin,
+                      const gbsimp_oc_params *prm, const float *x, const float *dc,
+                      const uint8_t *preserved, float *xnew, float *xphys, void *stream);
 /* Synchronises the stream; returns lambda and bisection steps of the last gbsimp_oc. */
 int gbsimp_oc_result(gbsimp_ctx *ctx, const void *ws, double *lambda_out, int *steps_out,
                      void *stream);
