@@ -93,13 +93,28 @@ __device__ __forceinline__ void modal_element(float (&v)[8][3], float E, const M
         for (int c = 0; c < 3; ++c) v[b][c] = r[b][c];
 }
 
+// PCG operands of one pass: p_new = r * dinv + beta * p_old is formed on the staged planes,
+// x += alpha_prev * p_old on the owned nodes, p_new is written for the owned nodes.
+struct PcgPass {
+    float beta, alpha_prev;
+    const float *r, *dinv, *pold;
+    float *pnew, *xu;
+};
+
+template <int MODE>
+__device__ __forceinline__ float ld_vec(const float *p) {
+    if (MODE == MODE_FUSED) return __ldcg(p);
+    return *p;
+}
+
+// One sliding-window pass of a CTA over its (flat tile, x segment): y = D K D p on the owned
+// nodes. Returns this thread's share of p.y (PCG mode; 0 otherwise).
 template <int NT, int EPT, int MAXN, int MODE>
-__global__ void __launch_bounds__(NT, 2)
-    apply_modal_kernel(ModalGeom G, const float *__restrict__ x, const float *__restrict__ p, float *__restrict__ y,
-                       const uint8_t *__restrict__ mask, Law<float> law, const ModalK km, PcgArgs pa) {
+__device__ __forceinline__ double modal_pass(const ModalGeom &G, const float *__restrict__ x,
+                                             const float *__restrict__ p, float *__restrict__ y,
+                                             const uint8_t *__restrict__ mask, const Law<float> &law,
+                                             const ModalK &km, const PcgPass &pp, float4 *smem4) {
     constexpr int NE = NT * EPT;
-    extern __shared__ float4 smem4[];
-    __shared__ double sred[32];
 
     const int nx = G.nx, ny = G.ny, nz = G.nz;
     const int NZ = nz + 1;
@@ -116,18 +131,9 @@ __global__ void __launch_bounds__(NT, 2)
     float *Es = (float *)(Pn + 3 * R);  // [2][NE] element moduli
     float *Cc = Es + 2 * NE;            // [24][NE] element corner contributions
 
-    int it = 0;
-    float beta = 0.0f, alpha_prev = 0.0f;
-    const float *pold = nullptr;
-    float *pnew = nullptr;
-    if (MODE == MODE_PCG) {
-        if (pa.sc->done) return;
-        it = pa.sc->iter;
-        beta = (float)pa.sc->beta;
-        alpha_prev = (float)pa.sc->alpha[(it + 1) & 1];
-        pold = (it & 1) ? pa.pbuf0 : pa.pbuf1;
-        pnew = (it & 1) ? pa.pbuf1 : pa.pbuf0;
-    }
+    const float beta = pp.beta, alpha_prev = pp.alpha_prev;
+    const float *pold = pp.pold;
+    float *pnew = pp.pnew;
 
     // ---- staging: issue the loads of a plane now, combine and store them later, so that
     // the element work of the current plane hides their latency ------------------------
@@ -147,9 +153,9 @@ __global__ void __launch_bounds__(NT, 2)
                 if (MODE == MODE_PLAIN) {
                     ra[q][c] = ok ? p[3 * n + c] : 0.0f;
                 } else {
-                    ra[q][c] = ok ? pa.r[3 * n + c] : 0.0f;
-                    rb[q][c] = ok ? pa.dinv[3 * n + c] : 0.0f;
-                    rc[q][c] = ok ? pold[3 * n + c] : 0.0f;
+                    ra[q][c] = ok ? ld_vec<MODE>(&pp.r[3 * n + c]) : 0.0f;
+                    rb[q][c] = ok ? pp.dinv[3 * n + c] : 0.0f;
+                    rc[q][c] = ok ? ld_vec<MODE>(&pold[3 * n + c]) : 0.0f;
                 }
             }
             if (MODE == MODE_PLAIN) rm[q] = (ok && mask) ? mask[n] : (uint8_t)0;
@@ -218,9 +224,9 @@ __global__ void __launch_bounds__(NT, 2)
             om[q] = (ok && mask) ? mask[n] : (uint8_t)0;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                if (MODE == MODE_PCG) {
-                    ox[q][c] = ok ? pa.xu[3 * n + c] : 0.0f;
-                    op[q][c] = ok ? pold[3 * n + c] : 0.0f;
+                if (MODE != MODE_PLAIN) {
+                    ox[q][c] = ok ? ld_vec<MODE>(&pp.xu[3 * n + c]) : 0.0f;
+                    op[q][c] = ok ? ld_vec<MODE>(&pold[3 * n + c]) : 0.0f;
                 } else {
                     ox[q][c] = op[q][c] = 0.0f;
                 }
@@ -285,10 +291,10 @@ __global__ void __launch_bounds__(NT, 2)
                     for (int c = 0; c < 3; ++c) {
                         const float yc = ((om[q] >> c) & 1) ? 0.0f : yv[c];
                         y[3 * n + c] = yc;
-                        if (MODE == MODE_PCG) {
+                        if (MODE != MODE_PLAIN) {
                             pnew[3 * n + c] = pc[c];
                             part += (double)(pc[c] * yc);
-                            pa.xu[3 * n + c] = fmaf(alpha_prev, op[q][c], ox[q][c]);
+                            pp.xu[3 * n + c] = fmaf(alpha_prev, op[q][c], ox[q][c]);
                         }
                     }
                 }
@@ -299,6 +305,27 @@ __global__ void __launch_bounds__(NT, 2)
         __syncthreads();
     }
 
+    return part;
+}
+
+template <int NT, int EPT, int MAXN, int MODE>
+__global__ void __launch_bounds__(NT, 2)
+    apply_modal_kernel(ModalGeom G, const float *__restrict__ x, const float *__restrict__ p, float *__restrict__ y,
+                       const uint8_t *__restrict__ mask, Law<float> law, const ModalK km, PcgArgs pa) {
+    extern __shared__ float4 smem4[];
+    __shared__ double sred[32];
+    const int tid = threadIdx.x;
+    int it = 0;
+    PcgPass pp{0.0f, 0.0f, pa.r, pa.dinv, nullptr, nullptr, pa.xu};
+    if (MODE == MODE_PCG) {
+        if (pa.sc->done) return;
+        it = pa.sc->iter;
+        pp.beta = (float)pa.sc->beta;
+        pp.alpha_prev = (float)pa.sc->alpha[(it + 1) & 1];
+        pp.pold = (it & 1) ? pa.pbuf0 : pa.pbuf1;
+        pp.pnew = (it & 1) ? pa.pbuf1 : pa.pbuf0;
+    }
+    const double part = modal_pass<NT, EPT, MAXN, MODE>(G, x, p, y, mask, law, km, pp, smem4);
     if (MODE == MODE_PCG) {
         const double bs = block_sum(part, sred);
         const int nblk = gridDim.x * gridDim.y;

@@ -20,7 +20,9 @@
 
 namespace gbs {
 
-enum { MODE_PLAIN = 0, MODE_PCG = 1 };
+// MODE_FUSED: the PCG pass inside the persistent kernel; vectors that other CTAs rewrite
+// between passes are read at L2 (L1 is not coherent across SMs within one launch).
+enum { MODE_PLAIN = 0, MODE_PCG = 1, MODE_FUSED = 2 };
 
 // Device-resident state of one Jacobi-PCG solve (FP32 vectors, FP64 scalars).
 struct PcgScalars {
@@ -36,6 +38,7 @@ struct PcgScalars {
     int status;       // GBS_OK / GBS_ENOTCONV / GBS_EBREAKDOWN / GBS_ENONFINITE
     int max_iter;
     unsigned counter; // blocks finished in the running kernel (last-block reductions)
+    unsigned bar_count, bar_gen;  // grid barrier of the persistent kernel
     int trips;        // WHILE-loop trips run by the device-driven loop
     int max_trips;    // hard cap on those trips (the loop always ends)
     int pad;

@@ -239,6 +239,217 @@ static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const La
 }
 
 // FP32 PCG. u: x0 in, solution out. Returns GBS_OK and fills *out (status inside).
+// ---- persistent fused PCG: the whole solve in one cooperative launch ---------------------
+// Every CTA keeps its (flat tile, x segment) of the modal apply for all iterations. One
+// iteration = the PCG apply pass (p = z + beta p, x += alpha p_old, Ap, p.Ap) -> grid
+// barrier that reduces p.Ap to alpha -> r -= alpha Ap on the owned nodes with r.r, r.z ->
+// grid barrier that reduces them to beta and the stop test. The last CTA to arrive at a
+// barrier does the fixed-order reduction and releases the others. Each wait is bounded in
+// time (%globaltimer): on expiry the CTA records GBS_ETIMEOUT, sets done and leaves.
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid-wide sums at a barrier. Each block publishes its K block sums in slot `slot` (two
+// slots alternate: a block can only reach the next use of a slot after every block has left
+// the barrier that last read it), arrives on a monotonic counter and waits for `target`
+// arrivals; then every block sums all partials itself in block order, so every block holds
+// the same totals (no serial finisher, deterministic). Waits are bounded by wait_ns.
+template <int K>
+__device__ bool grid_sums(const double (&v)[K], double *partials, int slot, unsigned *count, unsigned target, int nblk,
+                          int bid, unsigned long long wait_ns, double *sred, double (&tot)[K]) {
+    __shared__ bool s_ok;
+    __shared__ double s_tot[K];
+    double bs[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) bs[k] = block_sum(v[k], sred);
+    double *part = partials + (size_t)slot * K * nblk;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) part[k * nblk + bid] = bs[k];
+        __threadfence();
+        atomicAdd(count, 1u);
+        s_ok = true;
+        const unsigned long long t0 = global_ns();
+        while (*(volatile unsigned *)count < target) {
+            if (global_ns() - t0 > wait_ns) {
+                s_ok = false;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    if (!s_ok) return false;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double s = 0.0;
+        for (int i = threadIdx.x; i < nblk; i += blockDim.x) s += __ldcg(&part[k * nblk + i]);
+        s = block_sum(s, sred);
+        if (threadIdx.x == 0) s_tot[k] = s;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) tot[k] = s_tot[k];
+    return true;
+}
+
+template <int NT, int EPT, int MAXN>
+__global__ void __launch_bounds__(NT, 2)
+    pcg_fused_kernel(ModalGeom G, const float *__restrict__ x, const uint8_t *__restrict__ mask, Law<float> law,
+                     const ModalK km, PcgArgs pa, float *ap, unsigned long long wait_ns) {
+    extern __shared__ float4 smem4[];
+    __shared__ double sred[32];
+    PcgScalars *sc = pa.sc;
+    const int nz = G.nz, NZ = nz + 1, S = (G.ny + 1) * NZ;
+    const int F = NT * EPT - (nz + 2);
+    const int F0 = blockIdx.x * F;
+    const int nf = max(0, min(F, S - F0));
+    const int xs = blockIdx.y * G.seglen;
+    const int np = max(0, min(xs + G.seglen, G.nx + 1) - xs);
+    const int owned = nf * np;
+    const int nblk = gridDim.x * gridDim.y;
+    const int bid = blockIdx.x + gridDim.x * blockIdx.y;
+    // The solve's scalars, identical in every block (each block computes them itself).
+    const volatile PcgScalars *vsc = sc;
+    int it = vsc->iter, done = vsc->done, status = vsc->status;
+    double rz = vsc->rz, beta = vsc->beta, alpha_prev = vsc->alpha[(it + 1) & 1], rr = vsc->rr;
+    const double tol = vsc->tol, bnorm = vsc->bnorm;
+    const int max_iter = vsc->max_iter;
+    unsigned target = 0;
+    double alpha = 0.0, pap = 0.0;
+    while (!done) {
+        PcgPass pp;
+        pp.beta = (float)beta;
+        pp.alpha_prev = (float)alpha_prev;
+        pp.r = pa.r;
+        pp.dinv = pa.dinv;
+        pp.pold = (it & 1) ? pa.pbuf0 : pa.pbuf1;
+        pp.pnew = (it & 1) ? pa.pbuf1 : pa.pbuf0;
+        pp.xu = pa.xu;
+        const double part = modal_pass<NT, EPT, MAXN, MODE_FUSED>(G, x, nullptr, ap, mask, law, km, pp, smem4);
+        __threadfence();
+        target += nblk;
+        double t1[1];
+        const double v1[1] = {part};
+        if (!grid_sums<1>(v1, pa.partials, 0, &sc->bar_count, target, nblk, bid, wait_ns, sred, t1)) {
+            status = GBS_ETIMEOUT;
+            break;
+        }
+        pap = t1[0];
+        if (!(pap > 0.0) || !isfinite(pap)) {
+            status = isfinite(pap) ? GBS_EBREAKDOWN : GBS_ENONFINITE;
+            alpha = 0.0;
+            done = 1;
+            break;
+        }
+        alpha = rz / pap;
+        const float af = (float)alpha;
+        float rzf = 0.0f, rrf = 0.0f;
+        for (int q = threadIdx.x; q < owned; q += NT) {
+            const int64_t n = (int64_t)(xs + q / nf) * S + F0 + q % nf;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const int64_t d = 3 * n + c;
+                const float rd = fmaf(-af, __ldcg(&ap[d]), __ldcg(&pa.r[d]));
+                const_cast<float *>(pa.r)[d] = rd;
+                rrf = fmaf(rd, rd, rrf);
+                rzf = fmaf(rd * pa.dinv[d], rd, rzf);
+            }
+        }
+        __threadfence();
+        target += nblk;
+        double t2[2];
+        const double v2[2] = {(double)rzf, (double)rrf};
+        if (!grid_sums<2>(v2, pa.partials, 1, &sc->bar_count, target, nblk, bid, wait_ns, sred, t2)) {
+            status = GBS_ETIMEOUT;
+            break;
+        }
+        it += 1;
+        rr = t2[1];
+        if (!isfinite(t2[0]) || !isfinite(t2[1])) {
+            status = GBS_ENONFINITE;
+            done = 1;
+        } else if (sqrt(t2[1]) < tol * bnorm) {
+            done = 1;
+        } else if (it >= max_iter) {
+            status = GBS_ENOTCONV;
+            done = 1;
+        }
+        beta = t2[0] / rz;
+        rz = t2[0];
+        alpha_prev = alpha;
+    }
+    // Publish the final scalars (same values in every block; block 0 writes them). A block
+    // that timed out records the timeout itself.
+    if (status == GBS_ETIMEOUT) {
+        if (threadIdx.x == 0) {
+            atomicExch(&sc->status, (int)GBS_ETIMEOUT);
+            atomicExch(&sc->done, 1);
+        }
+        return;
+    }
+    if (bid == 0 && threadIdx.x == 0) {
+        sc->iter = it;
+        sc->done = 1;
+        sc->status = status;
+        sc->rz = rz;
+        sc->rr = rr;
+        sc->beta = beta;
+        sc->pap = pap;
+        // the finalize kernel adds alpha_{last} p_{last}: p_{it-1} lives in buffer (it-1)&1
+        sc->alpha[(it - 1) & 1] = status == GBS_EBREAKDOWN || status == GBS_ENONFINITE ? 0.0 : alpha;
+    }
+}
+
+// Runs the remaining iterations of an initialised PCG state in one cooperative launch.
+// Returns GBS_OK when launched, GBS_EINVAL when this grid cannot be co-resident (the caller
+// then uses the graph loop).
+static int pcg_fused_launch(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
+                            const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st) {
+    if (!(ctx->modal_ok && modal_fits(nz))) return GBS_EINVAL;
+    const bool small = modal_small_halo(nz);
+    void *kern = small ? (void *)pcg_fused_kernel<kModalNT, kModalEPT, kModalEPT + 1>
+                       : (void *)pcg_fused_kernel<kModalNT, kModalEPT, kModalEPT + 2>;
+    static int per_sm_cache[2][128] = {};
+    const int dev = ctx->device >= 0 && ctx->device < 128 ? ctx->device : 0;
+    int &per_sm = per_sm_cache[small ? 0 : 1][dev];
+    const int smax = (int)modal_smem_bytes<kModalNT, kModalEPT>(446);
+    if (per_sm == 0) {
+        int v = 0, coop = 0;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, kModalNT, smax) != cudaSuccess ||
+            cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
+            v = -1;
+        cudaGetLastError();
+        per_sm = v > 0 ? v : -1;
+    }
+    if (per_sm < 1) return GBS_EINVAL;
+    const ModalGeom g = modal_geom(nx, ny, nz, ctx->num_sms, per_sm);
+    const dim3 grid = modal_grid(g);
+    if ((long long)grid.x * grid.y > (long long)per_sm * ctx->num_sms) return GBS_EINVAL;
+    const size_t smem = modal_smem_bytes<kModalNT, kModalEPT>(nz);
+    PcgArgs pa{w.r, w.dinv, w.p0, w.p1, u, w.partials, w.sc};
+    float *ap = w.ap;
+    unsigned long long wait_ns = 2000000000ull;  // 2 s per barrier wait
+    ModalGeom gg = g;
+    Law<float> lw = law;
+    ModalK km = ctx->km;
+    const float *xx = x;
+    const uint8_t *mm = mask;
+    void *args[] = {&gg, &xx, &mm, &lw, &km, &pa, &ap, &wait_ns};
+    const cudaError_t e = cudaLaunchCooperativeKernel(kern, grid, dim3(kModalNT), args, smem, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();  // a refused launch must not surface at the next launch check
+        return set_error(GBS_EINVAL, "cooperative launch refused: %s", cudaGetErrorString(e));
+    }
+    count_launches(1);
+    return GBS_OK;
+}
+
 // ---- device-driven PCG loop: one CUDA graph with a WHILE node ------------------------------
 // Body: kLoopUnroll x (K1, K2) and a one-thread kernel that sets the loop condition from
 // the device flag `done`. K1/K2 return at once when done is set, so a finished solve costs
@@ -389,7 +600,7 @@ struct ApplyProfile {
 
 int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x, const float *b,
             const uint8_t *mask, float *u, double rtol, int max_iter, int check_every, void *ws, PcgScalars *out,
-            cudaStream_t st, ApplyProfile *prof = nullptr) {
+            cudaStream_t st, ApplyProfile *prof = nullptr, int fused = 0) {
     const int64_t nd = n_dof_of(nx, ny, nz);
     PcgWs w = pcg_ws(ws, nx, ny, nz);
     const Law<float> law = make_law<float>(*glaw);
@@ -404,6 +615,17 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
     PcgScalars h;
     rc = read_scalars(w.sc, &h, st);
     if (rc) return rc;
+    if (!prof && !h.done && fused) {
+        if (pcg_fused_launch(ctx, nx, ny, nz, law, x, mask, u, w, st) == GBS_OK) {
+            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc);
+            GBS_LAUNCH_CHECK("pcg_finalize_kernel");
+            rc = read_scalars(w.sc, &h, st);
+            if (rc) return rc;
+            *out = h;
+            return GBS_OK;
+        }
+        // the grid cannot be co-resident here: use the graph loop
+    }
     if (!prof && !h.done) {
         cudaGraphExec_t exec = nullptr;
         if (loop_graph(ctx, nx, ny, nz, law, x, mask, u, w, &exec) == GBS_OK) {
@@ -592,7 +814,7 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
         if (itol < inner) itol = inner;
         PcgScalars ps;
         rc = pcg_run(ctx, nx, ny, nz, law, x, w.b32, mask, w.d32, itol, o->max_iter - total, o->check_every, w.pcg,
-                     &ps, st, o->profile ? &prof : nullptr);
+                     &ps, st, o->profile ? &prof : nullptr, o->fused);
         if (rc) return rc;
         total += ps.iter;
         if (ps.status == GBS_EBREAKDOWN || ps.status == GBS_ENONFINITE) {
@@ -666,7 +888,7 @@ __global__ void csr_z_kernel(int64_t n, const float *__restrict__ r, const float
     double rz = 0.0;
     const float beta = set_p ? 0.0f : (float)sc->beta;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float zi = r[i] / diag[i];
+        const float zi = diag[i] != 0.0f ? r[i] / diag[i] : 0.0f;  // a zero diagonal entry (fixed row) gives z = 0
         z[i] = zi;
         rz += (double)r[i] * (double)zi;
     }
@@ -873,7 +1095,7 @@ extern "C" int gbsimp_pcg_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbs
     PcgScalars h;
     ApplyProfile prof;
     int rc = pcg_run(ctx, nx, ny, nz, law, x, b, node_mask, u, opts->rtol, opts->max_iter, opts->check_every, ws, &h,
-                     (cudaStream_t)stream, opts->profile ? &prof : nullptr);
+                     (cudaStream_t)stream, opts->profile ? &prof : nullptr, opts->fused);
     if (rc) return rc;
     if (stats) {
         stats->apply_seconds = prof.seconds;

@@ -214,7 +214,8 @@ class Engine:
                            int(fused), int(profile), 0)
 
     def pcg(self, grid: Grid, law: L.Law, x: torch.Tensor, b: torch.Tensor, mask: Optional[torch.Tensor],
-            u: torch.Tensor, rtol=1e-6, max_iter=2000, check_every=0, key: str = "pcg", profile=False) -> dict:
+            u: torch.Tensor, rtol=1e-6, max_iter=2000, check_every=0, key: str = "pcg", profile=False,
+            fused=False) -> dict:
         nx, ny, nz = grid
         nd = n_dof(grid)
         _need(x, torch.float32, n_elem(grid), "x")
@@ -223,7 +224,7 @@ class Engine:
         nb = self.lib.gbsimp_pcg_ws_bytes(nx, ny, nz)
         ws = self.workspace(key, nb)
         st = L.SolveStats()
-        o = self.opts(rtol=rtol, max_iter=max_iter, check_every=check_every, profile=int(profile))
+        o = self.opts(rtol=rtol, max_iter=max_iter, check_every=check_every, profile=int(profile), fused=int(fused))
         L.check(self.lib.gbsimp_pcg_f32(self.ctx, nx, ny, nz, C.byref(law), _p(x), _p(b), _p(mask), _p(u), C.byref(o),
                                         C.byref(st), _p(ws), nb, _stream()))
         return st.as_dict()
@@ -242,7 +243,7 @@ class Engine:
 
     def solve(self, grid: Grid, law: L.Law, x: torch.Tensor, f: torch.Tensor, mask: Optional[torch.Tensor],
               u: torch.Tensor, rtol=1e-8, inner_rtol=1e-3, max_iter=100000, max_outer=30, check_every=0,
-              key: str = "solve", profile=False) -> dict:
+              key: str = "solve", profile=False, fused=False) -> dict:
         nx, ny, nz = grid
         nd = n_dof(grid)
         _need(x, torch.float32, n_elem(grid), "x")
@@ -252,7 +253,7 @@ class Engine:
         ws = self.workspace(key, nb)
         st = L.SolveStats()
         o = self.opts(rtol=rtol, inner_rtol=inner_rtol, max_iter=max_iter, max_outer=max_outer,
-                      check_every=check_every, profile=int(profile))
+                      check_every=check_every, profile=int(profile), fused=int(fused))
         L.check(self.lib.gbsimp_solve(self.ctx, nx, ny, nz, C.byref(law), _p(x), _p(f), _p(mask), _p(u), C.byref(o),
                                       C.byref(st), _p(ws), nb, _stream()))
         return st.as_dict()

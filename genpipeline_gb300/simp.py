@@ -38,6 +38,7 @@ class SolveSpec:
     inner_rtol: float = 1e-3    # FP32 PCG reduction per outer correction
     max_iter: int = 200000
     max_outer: int = 30
+    fused: bool = False         # persistent one-launch PCG (grid barriers) instead of the graph loop
 
     def material(self) -> L.Law:
         return L.make_law(self.law, self.penal, self.e0, self.emin, self.xmin)
@@ -95,7 +96,7 @@ class SimpProblem:
         return self.eng.solve(self.grid, self.law, self.xphys, self.f, self.mask, self.u,
                               rtol=s.rtol if rtol is None else rtol, inner_rtol=s.inner_rtol,
                               max_iter=s.max_iter, max_outer=s.max_outer, key=f"solve:{id(self)}",
-                              profile=self.profile)
+                              profile=self.profile, fused=s.fused)
 
     def step(self) -> dict:
         """One OC iteration of the reference loop."""

@@ -1,0 +1,214 @@
+"""The drop-in classes and functions against the reference's own results and the oracle."""
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from genpipeline_gb300 import _lib as L
+from genpipeline_gb300 import bcs, cuda_kernels
+from genpipeline_gb300.fem import GPUConjugateGradientFEM, GPUVoxelFEM
+from genpipeline_gb300.topology import DenseGPUSolver, SIMPSolver, SIMPSolverGPU
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+# ---- SIMPSolver (genpipeline/topology/simp_solver.py) ------------------------------------
+def test_simp_solver_reproduces_reference_trajectories(golden):
+    """Whole SIMPSolver.run trajectories of the reference (SPD element injected) on small
+    grids: FP32 densities/filter/OC on the GPU against FP64 spsolve on the CPU."""
+    g = golden("simp_small")
+    for name, c in json.loads(str(g["cases"])).items():
+        nx, ny, nz = c["grid"]
+        pres = g[name + "_preserved"].reshape(nx, ny, nz) if c["preserved"] else None
+        s = SIMPSolver(nx, ny, nz, penal=c["penal"], rmin=c["rmin"], boundary_conditions=c["bcs"],
+                       preserved_mask=pres)
+        xp = s.run(volfrac=c["volfrac"], n_iters=c["iters"], force_mag=c["force"])
+        assert xp.shape == (nx, ny, nz)
+        np.testing.assert_allclose(xp.ravel(), g[name + "_xphys"], rtol=0, atol=2e-4, err_msg=name)
+        assert s.last_compliance == pytest.approx(float(g[name + "_compliance"]), rel=2e-5), name
+
+
+def test_simp_solver_c0_fifty_iterations(golden):
+    """32x16x16, volfrac 0.3, rmin 1.5, penal 3, 50 iterations: the reference ends at
+    compliance 8.0604130461 (410 s on one CPU core)."""
+    path = os.path.join(os.path.dirname(__file__), "golden", "simp_c0.npz")
+    if not os.path.exists(path):
+        pytest.skip("simp_c0.npz not generated")
+    g = golden("simp_c0")
+    s = SIMPSolver(32, 16, 16, penal=3.0, rmin=1.5)
+    xp = s.run(volfrac=0.3, n_iters=50, force_mag=1.0)
+    assert s.last_compliance == pytest.approx(float(g["compliance"]), rel=1e-4)
+    assert np.abs(xp.ravel() - g["xphys"]).max() < 5e-3
+    assert abs(xp.mean() - 0.3) < 1e-3
+
+
+# ---- SIMPSolverGPU (genpipeline/topology/simp_solver_gpu.py) -----------------------------
+def test_simp_solver_gpu_bcs_and_oc_internals(golden):
+    gb = golden("bcs")
+    for (gx, gy, gz) in ((6, 4, 5), (7, 3, 8)):
+        for name, spec in json.loads(str(gb["gpu_cases"])).items():
+            tag = f"gpu_{gx}{gy}{gz}_{name}"
+            s = SIMPSolverGPU(gx, gy, gz, boundary_conditions=spec)
+            f, fixed = s._get_bcs(2.5)
+            np.testing.assert_allclose(f.cpu().numpy(), gb[tag + "_f"], atol=1e-15)
+            np.testing.assert_array_equal(np.unique(fixed.cpu().numpy()), gb[tag + "_fixed"])
+    gk = golden("kernels")
+    for rmin in (1.5, 2.0):
+        s = SIMPSolverGPU(6, 5, 4, rmin=rmin)
+        xn, xp = s._oc_update(torch.as_tensor(gk["oc_x"]).cuda(), None, torch.as_tensor(gk["oc_dc"]).cuda(), 0.3)
+        np.testing.assert_allclose(xn.cpu().numpy(), gk[f"ocgpu_r{rmin}_x"], rtol=1e-5, atol=1e-6)
+        np.testing.assert_allclose(xp.cpu().numpy(), gk[f"ocgpu_r{rmin}_xphys"], rtol=1e-5, atol=1e-6)
+
+
+def test_simp_solver_gpu_run_contract():
+    s = SIMPSolverGPU(16, 8, 8, penal=3.0, rmin=1.5)
+    xp = s.run(volfrac=0.35, n_iters=12, force_mag=1.0)
+    assert xp.shape == (16, 8, 8) and np.isfinite(xp).all()
+    assert abs(xp.mean() - 0.35) < 2e-3
+    # last_compliance is a fresh solve on the final design (simp_solver_gpu.py:111,135)
+    c = s._calculate_compliance(torch.as_tensor(xp).cuda(), 1.0)
+    assert s.last_compliance == pytest.approx(c, rel=1e-4)
+    assert s.history[-1] <= s.history[0]
+
+
+def test_simp_solver_gpu_x_init_and_preserved():
+    pres = np.zeros((12, 6, 6), dtype=bool)
+    pres[-2:, :, :2] = True
+    rng = np.random.default_rng(3)
+    s = SIMPSolverGPU(12, 6, 6, preserved_mask=pres)
+    xp = s.run(volfrac=0.4, n_iters=4, x_init=rng.uniform(0, 1, (12, 6, 6)))
+    assert np.all(xp[pres] == 1.0)
+
+
+def test_dense_gpu_solver_contract():
+    s = DenseGPUSolver(12, 6, 6, penal=3.0, rmin=1.5)
+    xp = s.run(volfrac=0.25, n_iters=5, force_mag=1000)
+    assert xp.shape == (12, 6, 6) and abs(xp.mean() - 0.25) < 2e-3 and s.last_compliance > 0
+
+
+# ---- GPUVoxelFEM (genpipeline/fem/gpu_fem_solver.py) ------------------------------------
+def test_gpu_voxel_fem_against_oracle():
+    vox = np.ones((20, 10, 10), dtype=np.float32)
+    vox[8:12, 3:7, 3:7] = 0.0
+    fem = GPUVoxelFEM(vox, fixed_face="x_min", load_face="x_max", load_dof=2, force_n=30.0)
+    r = fem.solve()
+    assert set(r) == {"stress_max", "displacement_max", "compliance"}
+    f, fixed = bcs.reference_gpu(20, 10, 10, None, 30.0)
+    E = O.moduli(vox.ravel().astype(np.float64), O.Material("ref", 1.0))
+    u, _, _ = O.pcg((20, 10, 10), O.ke_quadrature(), E, f, bcs.dof_mask(20, 10, 10, fixed), tol=1e-12)
+    c_ref = float(f @ u)
+    # tol 1e-3 / 200 iterations, as the reference solves (gpu_fem_solver.py:96)
+    assert r["compliance"] == pytest.approx(c_ref, rel=1e-2)
+    n_solid = int((vox > 0.5).sum())
+    assert r["stress_max"] == pytest.approx(min(r["compliance"] / n_solid * 10.0, 1e4))  # clipped at 1e4
+    assert GPUConjugateGradientFEM is GPUVoxelFEM
+
+
+def test_gpu_voxel_fem_sentinel_for_near_void_design():
+    vox = np.zeros((12, 6, 6), dtype=np.float32)
+    vox[:2, :2, :2] = 1.0
+    assert GPUVoxelFEM(vox).solve() == {"stress_max": 1e4, "displacement_max": 1e3, "compliance": 1e6}
+
+
+# ---- cuda_kernels (genpipeline/cuda_kernels/__init__.py) --------------------------------
+@pytest.fixture
+def sample_32x8x8():
+    """The fixture of the reference's kernel test (tests/test_aggressive_kernel.py:37-61):
+    random SPD Ke = R R^T, random u and a random element -> DOF table, seed 42."""
+    torch.manual_seed(42)
+    nx, ny, nz = 32, 8, 8
+    n = nx * ny * nz
+    n_dof = n * 24
+    xPhys = torch.rand(n, dtype=torch.float32, device="cuda")
+    u = torch.randn(n_dof, dtype=torch.float32, device="cuda")
+    R = torch.randn(24, 24, dtype=torch.float32, device="cuda")
+    Ke = R @ R.T
+    edof = torch.randint(0, n_dof, (n, 24), dtype=torch.int32, device="cuda")
+    return xPhys, u, Ke, edof, (nx, ny, nz)
+
+
+def _torch_sensitivity(xPhys, u, Ke, edof, penal):
+    ue = u[edof.long()].double()
+    ce = ((ue @ Ke.double()) * ue).sum(1)
+    return -penal * torch.clamp(xPhys.double(), min=1e-3) ** (penal - 1) * ce
+
+
+def test_kernel_sensitivity_shapes_and_agreement(sample_32x8x8):
+    xPhys, u, Ke, edof, (nx, ny, nz) = sample_32x8x8
+    a = cuda_kernels.simp_sensitivity(xPhys, u, Ke, edof, 3.0, nx, ny, nz)
+    b = cuda_kernels.simp_sensitivity_aggressive(xPhys, u, Ke, edof, 3.0, nx, ny, nz)
+    assert a.shape == xPhys.shape and a.dtype == xPhys.dtype
+    assert (a - b).abs().max().item() / (a.abs().max().item() + 1e-10) < 0.01
+    ref = _torch_sensitivity(xPhys, u, Ke, edof, 3.0)
+    np.testing.assert_allclose(a.double().cpu().numpy(), ref.cpu().numpy(), rtol=1e-4,
+                               atol=1e-5 * ref.abs().max().item())
+
+
+def test_kernel_sensitivity_zero_u_gives_zero():
+    nx = ny = nz = 4
+    n = nx * ny * nz
+    xPhys = torch.ones(n, device="cuda") * 0.5
+    u = torch.zeros(n * 24, device="cuda")
+    Ke = torch.eye(24, device="cuda")
+    edof = torch.arange(n * 24, dtype=torch.int32, device="cuda").reshape(n, 24)
+    r = cuda_kernels.simp_sensitivity_aggressive(xPhys, u, Ke, edof, 3.0, nx, ny, nz)
+    assert torch.allclose(r, torch.zeros_like(r), atol=1e-6)
+
+
+def test_kernel_fused_spmv_against_torch_scatter(sample_32x8x8):
+    xPhys, u, Ke, edof, (nx, ny, nz) = sample_32x8x8
+    y = cuda_kernels.fused_spmv(xPhys, u, Ke, edof, 3.0, nx, ny, nz)
+    E = torch.clamp(xPhys.double(), min=1e-3) ** 3
+    ye = (u[edof.long()].double() @ Ke.double().T) * E[:, None]
+    ref = torch.zeros(u.numel(), dtype=torch.float64, device="cuda").index_add_(0, edof.long().reshape(-1),
+                                                                                ye.reshape(-1))
+    np.testing.assert_allclose(y.double().cpu().numpy(), ref.cpu().numpy(), rtol=0,
+                               atol=1e-4 * ref.abs().max().item())
+
+
+def test_kernel_fused_spmv_structured_equals_apply():
+    """On the structured edof map, fused_spmv equals the matrix-free apply."""
+    from genpipeline_gb300.engine import Engine
+
+    nx, ny, nz = 5, 4, 3
+    e = np.arange(nx * ny * nz)
+    i, j, k = e // (ny * nz), (e // nz) % ny, e % nz
+    corners = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    edof = np.stack([3 * bcs.node_id(i + cx, j + cy, k + cz, ny, nz) + c for cx, cy, cz in corners for c in range(3)],
+                    axis=1)
+    x = torch.rand(nx * ny * nz, device="cuda")
+    p = torch.randn(3 * (nx + 1) * (ny + 1) * (nz + 1), device="cuda")
+    Ke = torch.as_tensor(Engine.ke_quadrature(), dtype=torch.float32, device="cuda")
+    y = cuda_kernels.fused_spmv(x, p, Ke, torch.as_tensor(edof, device="cuda"), 3.0, nx, ny, nz)
+    y2 = Engine().apply((nx, ny, nz), L.make_law("ref", 3.0), x, p)
+    np.testing.assert_allclose(y.cpu().numpy(), y2.cpu().numpy(), rtol=0, atol=1e-5 * y2.abs().max().item())
+
+
+def test_kernel_pcg_solve_cuda_against_dense_solve():
+    import scipy.sparse as sp
+
+    grid = (6, 4, 4)
+    nd = 3 * 7 * 5 * 5
+    rng = np.random.default_rng(0)
+    x = rng.uniform(0.2, 1.0, np.prod(grid))
+    E = O.moduli(x, O.Material("ref", 3.0))
+    ke = O.ke_quadrature()
+    cols = [O.apply(grid, ke, E, np.eye(nd)[c]) for c in range(nd)]  # K column by column
+    K = np.array(cols).T
+    f, fixed = bcs.cantilever_tip(*grid)
+    free = np.setdiff1d(np.arange(nd), fixed)
+    Kb = K.copy()
+    Kb[fixed, :] = 0.0
+    Kb[:, fixed] = 0.0
+    Kb[fixed, fixed] = 1.0
+    ref = np.zeros(nd)
+    ref[free] = np.linalg.solve(K[np.ix_(free, free)], f[free])
+    A = sp.csr_matrix(Kb)
+    t = lambda a, dt: torch.as_tensor(np.array(a), dtype=dt, device="cuda")
+    xs = cuda_kernels.pcg_solve_cuda(t(A.indptr, torch.int32), t(A.indices, torch.int32), t(A.data, torch.float32),
+                                     t(Kb.diagonal(), torch.float32), t(f, torch.float32), t(np.zeros(nd), torch.float32),
+                                     t(fixed, torch.int32), max_iter=2000, tol=1e-6)
+    np.testing.assert_allclose(xs.cpu().numpy(), ref, rtol=0, atol=1e-4 * np.abs(ref).max())

@@ -293,6 +293,38 @@ def test_device_loop_and_host_loop_agree_bitwise(eng):
     assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][0], res[2][0])
 
 
+@pytest.mark.parametrize("grid,case", [((24, 12, 12), "top_patch"), ((64, 32, 32), "cantilever"),
+                                       ((40, 20, 100), "edge_line")])
+def test_fused_persistent_pcg_matches_graph_loop(eng, grid, case):
+    """One cooperative launch for the whole inner PCG (grid barriers) against the graph loop
+    of two launches per iteration: same solution to the solve tolerance, iteration counts
+    within a few (the r.r / r.z partial sums are grouped differently)."""
+    f, fixed, x = _problem(grid, case)
+    m = _cuda(bcs.node_mask(*grid, fixed))
+    lw = L.make_law("modified", 3.0)
+    out = {}
+    for fused in (False, True):
+        u = torch.zeros(n_dof(grid), dtype=torch.float64, device="cuda")
+        st = eng.solve(grid, lw, _cuda(x), _cuda(f), m, u, rtol=1e-8, fused=fused)
+        assert st["status"] == L.GBS_OK and st["relres"] <= 1e-8, st
+        out[fused] = (u.cpu().numpy(), st["iterations"])
+    np.testing.assert_allclose(out[True][0], out[False][0], rtol=0, atol=1e-6 * np.abs(out[False][0]).max())
+    assert abs(out[True][1] - out[False][1]) <= max(5, 0.05 * out[False][1])
+
+
+def test_fused_pcg_is_deterministic(eng):
+    grid = (32, 16, 16)
+    f, fixed, x = _problem(grid)
+    m = _cuda(bcs.node_mask(*grid, fixed))
+    lw = L.make_law("modified", 3.0)
+    res = []
+    for _ in range(2):
+        u = torch.zeros(n_dof(grid), dtype=torch.float64, device="cuda")
+        eng.solve(grid, lw, _cuda(x), _cuda(f), m, u, rtol=1e-8, fused=True)
+        res.append(u.cpu().numpy())
+    assert np.array_equal(res[0], res[1])
+
+
 def test_time_pcg_apply(eng):
     grid = (32, 16, 16)
     f, fixed, x = _problem(grid)
