@@ -42,6 +42,8 @@ WORKLOADS = {
     "c0": {"workload": "simp_32x16x16_cantilever", "grid": [32, 16, 16], "rmin": 1.5, "volfrac": 0.3,
            "load": "cantilever", "load_text": "x=0 clamped, unit -z point load at node (32, 8, 0)"},
     # 192x96x96 (1,769,472 elements, 5,447,811 DOFs): the HBM-bound size of the apply
+    "serve": {"workload": "fem_serving_stream", "grid": [64, 64, 64], "rmin": 2.0, "volfrac": 0.25,
+              "load": "top_patch", "load_text": "per request: cantilever tip, top patch or torsion couple"},
     "c4": {"workload": "simp_192x96x96_edge_line", "grid": [192, 96, 96], "rmin": 3.0, "volfrac": 0.2,
            "load": "edge_line",
            "load_text": "x=0 clamped, -z line load (total 1) along the bottom edge of the x=192 face"},
@@ -60,6 +62,8 @@ def _args():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="simp64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-steps", type=int, default=1)
+    ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched FEM (served vs plain) measurement")
     ap.add_argument("--host-loop", action="store_true",
                     help="launch PCG iterations from the host (for kernel profilers) instead of the graph loop")
     return ap.parse_args()
@@ -178,6 +182,92 @@ def _cpu_threads():
     from oracle import oracle as O
 
     return O.num_threads()
+
+
+# ---- batched FEM evaluation: 8 designs (4 x 64^3 + 4 x 32^3), served vs plain --------------
+def batch_designs():
+    from genpipeline_gb300 import designs as D
+    from genpipeline_gb300.batch import FEMDesign
+
+    out = []
+    for k, n in enumerate((64, 64, 64, 64, 32, 32, 32, 32)):
+        f, fixed = D.cantilever_case(n)
+        out.append(FEMDesign((n, n, n), D.grf_density((n, n, n), k), f, fixed))
+    return out
+
+
+def measure_batch(repeats=2):
+    """FEM solves/s of the 8-design batch: plain = one solve per design (graph-loop PCG, one
+    design on the GPU at a time); served = the designs together in gbsimp_batch_round
+    (persistent kernel, each design on its share of the SMs). Cold starts (u0 = 0) both."""
+    import torch
+
+    from genpipeline_gb300.batch import BatchFEM, solve_plain
+
+    solve_plain(batch_designs())  # warm-up: graphs, code paths
+    BatchFEM().solve_all(batch_designs())
+    res = {}
+    for name in ("plain", "served"):
+        best = None
+        for _ in range(repeats):
+            ds = batch_designs()
+            bf = BatchFEM()
+            for d in ds:
+                bf.upload(d)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = solve_plain(ds) if name == "plain" else bf.solve_all(ds)
+            torch.cuda.synchronize()
+            t = time.perf_counter() - t0
+            if best is None or t < best[0]:
+                best = (t, {d.grid + (i,): d for i, d in enumerate(out)}, out)
+        res[name] = best
+    cp = sorted(d.compliance for d in res["plain"][2])
+    cs = sorted(d.compliance for d in res["served"][2])
+    diff = max(abs(a - b) / abs(a) for a, b in zip(cp, cs))
+    return {"workload": "8 designs: 4 x 64^3 + 4 x 32^3, GRF densities (length 6, mean U(0.2,0.5)), cantilever, "
+                        "FP32 PCG + FP64 correction to rtol 1e-8, cold start",
+            "plain": 8 / res["plain"][0], "served": 8 / res["served"][0],
+            "served_over_plain": res["plain"][0] / res["served"][0],
+            "max_compliance_rel_diff": diff,
+            "pcg_iterations": sum(d.stats["iterations"] for d in res["served"][2]),
+            "unit": "FEM solves/s"}
+
+
+def run_serve(a):
+    """Serving stream: Poisson arrivals at 200/s, edge U{24,32,48,64,96}, three load cases,
+    ~10% repeated designs; continuous batching with admission by free HBM."""
+    import torch
+
+    from genpipeline_gb300 import _lib as L
+    from genpipeline_gb300.serve import FEMServer, request_stream
+
+    lib = L.load()
+    warm = FEMServer(max_slots=8)
+    warm.run(request_stream(40, rate=1000.0, seed=99), realtime=False)
+    reqs = request_stream(a.serve_requests, rate=200.0)
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    l0 = lib.gbsimp_launch_count()
+    srv = FEMServer(max_slots=24)
+    summ = srv.run(reqs, realtime=True)
+    launches = lib.gbsimp_launch_count() - l0
+    clk = clocks.stop()
+    plain_reqs = request_stream(a.serve_requests, rate=200.0)[: max(50, a.serve_requests // 10)]
+    plain = FEMServer(max_slots=1).run(plain_reqs, realtime=False)
+    line = {"metric": METRIC, "value": summ["solves_per_s"], "unit": "FEM solves/s", "n_gpus": 1,
+            "steps": summ["requests"], "warmup": 40, "ms_per_step": 1e3 / summ["solves_per_s"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (FP64 outer residual, dots, compliance)", "data": "synthetic", "impl": "ours",
+            "config": {"workload": "fem_serving_stream", "requests": summ["requests"], "rate_per_s": 200.0,
+                       "edges": [24, 32, 48, 64, 96], "loads": ["cantilever", "top_patch", "torsion"],
+                       "repeat_fraction": 0.1, "rtol": 1e-8, "max_slots": 24},
+            "serving": summ, "plain_one_at_a_time": {"requests": plain["requests"], "solves_per_s": plain["solves_per_s"],
+                                                     "note": "same stream, all requests queued at t=0, one slot"},
+            "gpu_launches": int(launches), "clocks": clk,
+            "e2e": {"value": summ["solves_per_s"], "unit": "FEM solves/s",
+                    "h2d_bytes_per_step": None, "d2h_bytes_per_step": 8}}
+    print(json.dumps(line), flush=True)
 
 
 # ---- our arm -----------------------------------------------------------------------------
@@ -304,6 +394,10 @@ def run_ours(a):
                          f"GPU state after {a.warmup + 2 * a.steps} iterations (FP64 C/OpenMP oracle)",
                "seconds": tc}
 
+    fem = None
+    if rank == 0 and a.workload == "simp64" and not a.no_batch:
+        fem = measure_batch()
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": tmax / a.steps * 1e3, "higher_is_better": True,
@@ -314,7 +408,7 @@ def run_ours(a):
                                parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clk, "pcg_iterations_per_step": pcg_iters / a.steps,
-                "compliance_rel_err_vs_fp64_oracle": rel_err}
+                "compliance_rel_err_vs_fp64_oracle": rel_err, "fem_solves_per_s": fem}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -356,6 +450,8 @@ def main():
     a = _args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "serve":
+        run_serve(a)
     else:
         run_ours(a)
 

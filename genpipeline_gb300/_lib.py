@@ -67,6 +67,12 @@ class SolveStats(C.Structure):
                 "apply_seconds": float(self.apply_seconds), "apply_launches": int(self.apply_launches)}
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("state", C.c_int32),
+                ("x", C.c_void_p), ("f", C.c_void_p), ("node_mask", C.c_void_p), ("u", C.c_void_p),
+                ("ws", C.c_void_p), ("ws_bytes", C.c_size_t), ("stats", SolveStats)]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _I64 = C.c_int64
@@ -105,6 +111,8 @@ SIGNATURES = {
     "gbsimp_solve_ws_bytes": (_SZ, [_I, _I, _I]),
     "gbsimp_solve": (_I, [_P, _I, _I, _I, C.POINTER(Law), _P, _P, _P, _P, C.POINTER(SolveOpts),
                           C.POINTER(SolveStats), _P, _SZ, _P]),
+    "gbsimp_batch_round": (_I, [_P, C.POINTER(BatchItem), _I, C.POINTER(Law), C.POINTER(SolveOpts), _P]),
+    "gbsimp_batch_solve": (_I, [_P, C.POINTER(BatchItem), _I, C.POINTER(Law), C.POINTER(SolveOpts), _P]),
     "gbsimp_pcg_csr_ws_bytes": (_SZ, [_I64]),
     "gbsimp_pcg_csr_f32": (_I, [_P, _I64, _P, _P, _P, _P, _P, _P, _P, _I64, C.POINTER(SolveOpts),
                                 C.POINTER(SolveStats), _P, _SZ, _P]),

@@ -1,0 +1,127 @@
+"""Batched FEM solves: many designs of different sizes per launch (gbsimp_batch_round).
+
+The reference evaluates designs one at a time: ``VoxelFEMEvaluator.evaluate_batch`` fans
+``GPUVoxelFEM.solve`` calls out to a thread pool, and each call assembles its own CSR
+matrix and runs its own PCG loop (voxel_fem.py:559-611, gpu_fem_solver.py:76-133). Here a
+batch shares the GPU inside one persistent kernel per round. Every design gets a share of
+the SMs, its own grid barrier and its own scalars; the FP64 defect correction runs in
+lockstep rounds around those launches.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from . import bcs as B
+from .engine import Engine, get_engine, n_dof, n_elem
+
+
+@dataclass
+class FEMDesign:
+    """One forward solve: densities, load vector and fixed DOFs on a grid (host or device)."""
+
+    grid: tuple
+    x: np.ndarray
+    f: np.ndarray
+    fixed_dofs: np.ndarray
+    u0: Optional[torch.Tensor] = None  # warm start (FP64, device)
+    tag: object = None
+    # device state (filled by BatchFEM)
+    dx: Optional[torch.Tensor] = field(default=None, repr=False)
+    df: Optional[torch.Tensor] = field(default=None, repr=False)
+    dmask: Optional[torch.Tensor] = field(default=None, repr=False)
+    du: Optional[torch.Tensor] = field(default=None, repr=False)
+    ws: Optional[torch.Tensor] = field(default=None, repr=False)
+    stats: Optional[dict] = None
+    compliance: Optional[float] = None
+
+    def device_bytes(self, lib=None) -> int:
+        lib = lib or L.load()
+        nx, ny, nz = self.grid
+        return int(lib.gbsimp_solve_ws_bytes(nx, ny, nz)) + 4 * n_elem(self.grid) + 16 * n_dof(self.grid) + \
+            n_dof(self.grid) // 3
+
+
+class BatchFEM:
+    """Runs gbsimp_batch_round over a changing set of designs."""
+
+    def __init__(self, engine: Optional[Engine] = None, law: Optional[L.Law] = None, rtol: float = 1e-8,
+                 inner_rtol: float = 1e-3, max_iter: int = 200000, max_outer: int = 30, fused: bool = True):
+        self.eng = engine or get_engine()
+        self.law = law or L.make_law("modified", 3.0)
+        self.opts = Engine.opts(rtol=rtol, inner_rtol=inner_rtol, max_iter=max_iter, max_outer=max_outer,
+                                fused=int(fused))
+        self.items: List[FEMDesign] = []
+        self._structs = None
+
+    def upload(self, d: FEMDesign) -> FEMDesign:
+        dev = self.eng.device
+        nx, ny, nz = d.grid
+        d.dx = torch.as_tensor(np.asarray(d.x, dtype=np.float32).reshape(-1), device=dev).contiguous()
+        d.df = torch.as_tensor(np.asarray(d.f, dtype=np.float64), device=dev).contiguous()
+        d.dmask = torch.as_tensor(B.node_mask(nx, ny, nz, d.fixed_dofs), device=dev)
+        if d.u0 is not None:
+            d.du = d.u0.to(device=dev, dtype=torch.float64).clone().contiguous()
+        else:
+            d.du = torch.zeros(n_dof(d.grid), dtype=torch.float64, device=dev)
+        d.ws = torch.empty(int(self.eng.lib.gbsimp_solve_ws_bytes(nx, ny, nz)), dtype=torch.uint8, device=dev)
+        return d
+
+    def add(self, d: FEMDesign) -> FEMDesign:
+        if d.dx is None:
+            self.upload(d)
+        d._item = L.BatchItem(d.grid[0], d.grid[1], d.grid[2], 0, d.dx.data_ptr(), d.df.data_ptr(),
+                              d.dmask.data_ptr(), d.du.data_ptr(), d.ws.data_ptr(), d.ws.numel(), L.SolveStats())
+        self.items.append(d)
+        return d
+
+    def round(self) -> List[FEMDesign]:
+        """One defect-correction round for every active design; returns the designs that
+        finished in it (and drops them from the batch)."""
+        if not self.items:
+            return []
+        arr = (L.BatchItem * len(self.items))(*[d._item for d in self.items])
+        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        L.check(self.eng.lib.gbsimp_batch_round(self.eng.ctx, arr, len(self.items), C.byref(self.law),
+                                                C.byref(self.opts), stream))
+        done, keep = [], []
+        for i, d in enumerate(self.items):
+            d._item = arr[i]
+            if arr[i].state != 0:
+                d.stats = arr[i].stats.as_dict()
+                d.compliance = float(torch.dot(d.df, d.du).item())
+                done.append(d)
+            else:
+                keep.append(d)
+        self.items = keep
+        return done
+
+    def solve_all(self, designs: List[FEMDesign]) -> List[FEMDesign]:
+        for d in designs:
+            self.add(d)
+        out = []
+        for _ in range(int(self.opts.max_outer) + 2):
+            out += self.round()
+            if not self.items:
+                break
+        return out
+
+
+def solve_plain(designs: List[FEMDesign], engine: Optional[Engine] = None, law: Optional[L.Law] = None,
+                rtol: float = 1e-8, inner_rtol: float = 1e-3) -> List[FEMDesign]:
+    """The one-design-at-a-time form: one gbsimp_solve (graph-loop PCG) per design."""
+    eng = engine or get_engine()
+    law = law or L.make_law("modified", 3.0)
+    bf = BatchFEM(eng, law)
+    for d in designs:
+        if d.dx is None:
+            bf.upload(d)
+        d.stats = eng.solve(d.grid, law, d.dx, d.df, d.dmask, d.du, rtol=rtol, inner_rtol=inner_rtol,
+                            key=f"plain:{d.grid}")
+        d.compliance = float(torch.dot(d.df, d.du).item())
+    return designs

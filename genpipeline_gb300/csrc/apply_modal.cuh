@@ -113,7 +113,8 @@ template <int NT, int EPT, int MAXN, int MODE>
 __device__ __forceinline__ double modal_pass(const ModalGeom &G, const float *__restrict__ x,
                                              const float *__restrict__ p, float *__restrict__ y,
                                              const uint8_t *__restrict__ mask, const Law<float> &law,
-                                             const ModalK &km, const PcgPass &pp, float4 *smem4) {
+                                             const ModalK &km, const PcgPass &pp, float4 *smem4, int tile,
+                                             int seg) {
     constexpr int NE = NT * EPT;
 
     const int nx = G.nx, ny = G.ny, nz = G.nz;
@@ -122,8 +123,8 @@ __device__ __forceinline__ double modal_pass(const ModalGeom &G, const float *__
     const int H = nz + 2;         // flat halo (one y row plus one node)
     const int R = NE + H;         // staged nodes per plane
     const int F = NE - H;         // owned nodes per plane
-    const int F0 = blockIdx.x * F;
-    const int xs = blockIdx.y * G.seglen;
+    const int F0 = tile * F;
+    const int xs = seg * G.seglen;
     const int xe = min(xs + G.seglen, nx + 1);
     const int tid = threadIdx.x;
 
@@ -325,7 +326,7 @@ __global__ void __launch_bounds__(NT, 2)
         pp.pold = (it & 1) ? pa.pbuf0 : pa.pbuf1;
         pp.pnew = (it & 1) ? pa.pbuf1 : pa.pbuf0;
     }
-    const double part = modal_pass<NT, EPT, MAXN, MODE>(G, x, p, y, mask, law, km, pp, smem4);
+    const double part = modal_pass<NT, EPT, MAXN, MODE>(G, x, p, y, mask, law, km, pp, smem4, blockIdx.x, blockIdx.y);
     if (MODE == MODE_PCG) {
         const double bs = block_sum(part, sred);
         const int nblk = gridDim.x * gridDim.y;

@@ -11,6 +11,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <mutex>
 #include <string>
@@ -297,23 +298,46 @@ __device__ bool grid_sums(const double (&v)[K], double *partials, int slot, unsi
     return true;
 }
 
+// Designs of one cooperative launch. Each design owns the CTA range [block0, block0 + nblk)
+// laid out as `tiles` flat tiles x (nblk / tiles) x segments, its own PCG state and barrier
+// counter; designs advance independently.
+constexpr int kMaxFused = 24;
+struct FusedDesign {
+    ModalGeom G;
+    int tiles, block0, nblk, pad;
+    const float *x;
+    const uint8_t *mask;
+    float *ap;
+    PcgArgs pa;
+};
+struct FusedTable {
+    int n, pad;
+    FusedDesign d[kMaxFused];
+};
+
 template <int NT, int EPT, int MAXN>
 __global__ void __launch_bounds__(NT, 2)
-    pcg_fused_kernel(ModalGeom G, const float *__restrict__ x, const uint8_t *__restrict__ mask, Law<float> law,
-                     const ModalK km, PcgArgs pa, float *ap, unsigned long long wait_ns) {
+    pcg_fused_kernel(const __grid_constant__ FusedTable T, Law<float> law, const ModalK km,
+                     unsigned long long wait_ns) {
     extern __shared__ float4 smem4[];
     __shared__ double sred[32];
+    int di = 0;
+    while (di + 1 < T.n && (int)blockIdx.x >= T.d[di + 1].block0) ++di;
+    const FusedDesign &D = T.d[di];
+    const ModalGeom &G = D.G;
+    const PcgArgs &pa = D.pa;
+    const int bid = (int)blockIdx.x - D.block0;
+    const int nblk = D.nblk;
+    const int tile = bid % D.tiles, seg = bid / D.tiles;
     PcgScalars *sc = pa.sc;
     const int nz = G.nz, NZ = nz + 1, S = (G.ny + 1) * NZ;
     const int F = NT * EPT - (nz + 2);
-    const int F0 = blockIdx.x * F;
+    const int F0 = tile * F;
     const int nf = max(0, min(F, S - F0));
-    const int xs = blockIdx.y * G.seglen;
+    const int xs = seg * G.seglen;
     const int np = max(0, min(xs + G.seglen, G.nx + 1) - xs);
     const int owned = nf * np;
-    const int nblk = gridDim.x * gridDim.y;
-    const int bid = blockIdx.x + gridDim.x * blockIdx.y;
-    // The solve's scalars, identical in every block (each block computes them itself).
+    // The solve's scalars, identical in every block of the design (each block computes them).
     const volatile PcgScalars *vsc = sc;
     int it = vsc->iter, done = vsc->done, status = vsc->status;
     double rz = vsc->rz, beta = vsc->beta, alpha_prev = vsc->alpha[(it + 1) & 1], rr = vsc->rr;
@@ -330,7 +354,8 @@ __global__ void __launch_bounds__(NT, 2)
         pp.pold = (it & 1) ? pa.pbuf0 : pa.pbuf1;
         pp.pnew = (it & 1) ? pa.pbuf1 : pa.pbuf0;
         pp.xu = pa.xu;
-        const double part = modal_pass<NT, EPT, MAXN, MODE_FUSED>(G, x, nullptr, ap, mask, law, km, pp, smem4);
+        const double part =
+            modal_pass<NT, EPT, MAXN, MODE_FUSED>(G, D.x, nullptr, D.ap, D.mask, law, km, pp, smem4, tile, seg);
         __threadfence();
         target += nblk;
         double t1[1];
@@ -354,7 +379,7 @@ __global__ void __launch_bounds__(NT, 2)
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 const int64_t d = 3 * n + c;
-                const float rd = fmaf(-af, __ldcg(&ap[d]), __ldcg(&pa.r[d]));
+                const float rd = fmaf(-af, __ldcg(&D.ap[d]), __ldcg(&pa.r[d]));
                 const_cast<float *>(pa.r)[d] = rd;
                 rrf = fmaf(rd, rd, rrf);
                 rzf = fmaf(rd * pa.dinv[d], rd, rzf);
@@ -383,8 +408,6 @@ __global__ void __launch_bounds__(NT, 2)
         rz = t2[0];
         alpha_prev = alpha;
     }
-    // Publish the final scalars (same values in every block; block 0 writes them). A block
-    // that timed out records the timeout itself.
     if (status == GBS_ETIMEOUT) {
         if (threadIdx.x == 0) {
             atomicExch(&sc->status, (int)GBS_ETIMEOUT);
@@ -400,18 +423,34 @@ __global__ void __launch_bounds__(NT, 2)
         sc->rr = rr;
         sc->beta = beta;
         sc->pap = pap;
-        // the finalize kernel adds alpha_{last} p_{last}: p_{it-1} lives in buffer (it-1)&1
+        // the finalize kernel adds alpha_last p_last: p_{it-1} lives in buffer (it-1)&1
         sc->alpha[(it - 1) & 1] = status == GBS_EBREAKDOWN || status == GBS_ENONFINITE ? 0.0 : alpha;
     }
 }
 
-// Runs the remaining iterations of an initialised PCG state in one cooperative launch.
-// Returns GBS_OK when launched, GBS_EINVAL when this grid cannot be co-resident (the caller
-// then uses the graph loop).
-static int pcg_fused_launch(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
-                            const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st) {
-    if (!(ctx->modal_ok && modal_fits(nz))) return GBS_EINVAL;
-    const bool small = modal_small_halo(nz);
+// One design of a batched inner solve: an initialised PCG state (pcg_run's setup done).
+struct FusedItem {
+    int nx, ny, nz;
+    const float *x;
+    const uint8_t *mask;
+    float *u;
+    PcgWs w;
+};
+
+// Runs the remaining PCG iterations of up to kMaxFused initialised designs in one
+// cooperative launch. The CTAs of the GPU are shared in proportion to the designs' element
+// counts (at least one segment of flat tiles each). Returns GBS_EINVAL when the designs cannot
+// all be resident at once (the caller then iterates them with the graph loop).
+static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n, const Law<float> &law,
+                           cudaStream_t st) {
+    if (n <= 0 || n > kMaxFused || !ctx->modal_ok) return GBS_EINVAL;
+    bool small = true;
+    int max_nz = 0;
+    for (int i = 0; i < n; ++i) {
+        if (!modal_fits(items[i].nz)) return GBS_EINVAL;
+        small = small && modal_small_halo(items[i].nz);
+        max_nz = items[i].nz > max_nz ? items[i].nz : max_nz;
+    }
     void *kern = small ? (void *)pcg_fused_kernel<kModalNT, kModalEPT, kModalEPT + 1>
                        : (void *)pcg_fused_kernel<kModalNT, kModalEPT, kModalEPT + 2>;
     static int per_sm_cache[2][128] = {};
@@ -428,20 +467,60 @@ static int pcg_fused_launch(const gbsimp_ctx *ctx, int nx, int ny, int nz, const
         per_sm = v > 0 ? v : -1;
     }
     if (per_sm < 1) return GBS_EINVAL;
-    const ModalGeom g = modal_geom(nx, ny, nz, ctx->num_sms, per_sm);
-    const dim3 grid = modal_grid(g);
-    if ((long long)grid.x * grid.y > (long long)per_sm * ctx->num_sms) return GBS_EINVAL;
-    const size_t smem = modal_smem_bytes<kModalNT, kModalEPT>(nz);
-    PcgArgs pa{w.r, w.dinv, w.p0, w.p1, u, w.partials, w.sc};
-    float *ap = w.ap;
+    const int total = per_sm * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+    int tiles[kMaxFused], nseg[kMaxFused], seglen[kMaxFused];
+    double welem = 0.0;
+    int need = 0;
+    for (int i = 0; i < n; ++i) {
+        const int F = kModalNT * kModalEPT - (items[i].nz + 2);
+        const int S = (items[i].ny + 1) * (items[i].nz + 1);
+        tiles[i] = (S + F - 1) / F;
+        need += tiles[i];
+        welem += (double)items[i].nx * items[i].ny * items[i].nz;
+    }
+    if (need > total) return GBS_EINVAL;
+    int used = 0;
+    for (int i = 0; i < n; ++i) {
+        const double share = (double)items[i].nx * items[i].ny * items[i].nz / welem;
+        int s = (int)((double)total * share / tiles[i]);
+        s = s < 1 ? 1 : s;
+        if (s > items[i].nx + 1) s = items[i].nx + 1;
+        nseg[i] = s;
+        used += tiles[i] * s;
+    }
+    while (used > total) {  // trim the design with the most segments
+        int j = 0;
+        for (int i = 1; i < n; ++i)
+            if (nseg[i] > nseg[j]) j = i;
+        if (nseg[j] <= 1) return GBS_EINVAL;
+        nseg[j] -= 1;
+        used -= tiles[j];
+    }
+    FusedTable T;
+    memset(&T, 0, sizeof T);
+    T.n = n;
+    int block0 = 0;
+    for (int i = 0; i < n; ++i) {
+        const FusedItem &itm = items[i];
+        seglen[i] = (itm.nx + 1 + nseg[i] - 1) / nseg[i];
+        nseg[i] = (itm.nx + 1 + seglen[i] - 1) / seglen[i];
+        FusedDesign &D = T.d[i];
+        D.G = ModalGeom{itm.nx, itm.ny, itm.nz, nseg[i], seglen[i]};
+        D.tiles = tiles[i];
+        D.block0 = block0;
+        D.nblk = tiles[i] * nseg[i];
+        D.x = itm.x;
+        D.mask = itm.mask;
+        D.ap = itm.w.ap;
+        D.pa = PcgArgs{itm.w.r, itm.w.dinv, itm.w.p0, itm.w.p1, itm.u, itm.w.partials, itm.w.sc};
+        block0 += D.nblk;
+    }
+    const size_t smem = modal_smem_bytes<kModalNT, kModalEPT>(max_nz);
     unsigned long long wait_ns = 2000000000ull;  // 2 s per barrier wait
-    ModalGeom gg = g;
     Law<float> lw = law;
     ModalK km = ctx->km;
-    const float *xx = x;
-    const uint8_t *mm = mask;
-    void *args[] = {&gg, &xx, &mm, &lw, &km, &pa, &ap, &wait_ns};
-    const cudaError_t e = cudaLaunchCooperativeKernel(kern, grid, dim3(kModalNT), args, smem, st);
+    void *args[] = {&T, &lw, &km, &wait_ns};
+    const cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3((unsigned)block0), dim3(kModalNT), args, smem, st);
     if (e != cudaSuccess) {
         cudaGetLastError();  // a refused launch must not surface at the next launch check
         return set_error(GBS_EINVAL, "cooperative launch refused: %s", cudaGetErrorString(e));
@@ -591,6 +670,24 @@ static int loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<f
     return GBS_OK;
 }
 
+// PCG setup on the stream: zeroed scalars, 1/diag, q = D K D u, r = D b - q, z, p_{-1} = 0,
+// the first dot products and the stop test (nothing is read back).
+static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x,
+                     const float *b, const uint8_t *mask, float *u, double rtol, int max_iter, const PcgWs &w,
+                     cudaStream_t st) {
+    const int64_t nd = n_dof_of(nx, ny, nz);
+    const Law<float> law = make_law<float>(*glaw);
+    GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
+    dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, law, ctx->kef, x, mask, w.dinv);
+    GBS_LAUNCH_CHECK("dinv_kernel");
+    int rc = apply_f32(ctx, nx, ny, nz, glaw, x, u, w.ap, mask, st);
+    if (rc) return rc;
+    pcg_init_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, b, w.ap, mask, w.dinv, w.r, w.p1, u, w.partials, w.sc, rtol,
+                                                        max_iter, (max_iter + kLoopUnroll - 1) / kLoopUnroll + 2);
+    GBS_LAUNCH_CHECK("pcg_init_kernel");
+    return GBS_OK;
+}
+
 // Optional profiling (prof != nullptr): CUDA events around every K1 launch; only the
 // launches of iterations that actually ran (the device counter advanced) are summed.
 struct ApplyProfile {
@@ -604,19 +701,14 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
     const int64_t nd = n_dof_of(nx, ny, nz);
     PcgWs w = pcg_ws(ws, nx, ny, nz);
     const Law<float> law = make_law<float>(*glaw);
-    GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
-    dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, law, ctx->kef, x, mask, w.dinv);
-    GBS_LAUNCH_CHECK("dinv_kernel");
-    int rc = apply_f32(ctx, nx, ny, nz, glaw, x, u, w.ap, mask, st);
+    int rc = pcg_setup(ctx, nx, ny, nz, glaw, x, b, mask, u, rtol, max_iter, w, st);
     if (rc) return rc;
-    pcg_init_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, b, w.ap, mask, w.dinv, w.r, w.p1, u, w.partials, w.sc, rtol,
-                                                        max_iter, (max_iter + kLoopUnroll - 1) / kLoopUnroll + 2);
-    GBS_LAUNCH_CHECK("pcg_init_kernel");
     PcgScalars h;
     rc = read_scalars(w.sc, &h, st);
     if (rc) return rc;
     if (!prof && !h.done && fused) {
-        if (pcg_fused_launch(ctx, nx, ny, nz, law, x, mask, u, w, st) == GBS_OK) {
+        const FusedItem item{nx, ny, nz, x, mask, u, w};
+        if (pcg_fused_batch(ctx, &item, 1, law, st) == GBS_OK) {
             pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc);
             GBS_LAUNCH_CHECK("pcg_finalize_kernel");
             rc = read_scalars(w.sc, &h, st);
@@ -1185,5 +1277,184 @@ extern "C" int gbsimp_pcg_csr_f32(gbsimp_ctx *ctx, int64_t n, const int32_t *row
         stats->relres = h.bnorm > 0.0 ? sqrt(h.rr) / h.bnorm : 0.0;
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
+    return GBS_OK;
+}
+
+// ---- batched rounds ------------------------------------------------------------------------
+namespace gbs {
+
+static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int n, const gbsimp_law *glaw,
+                            const gbsimp_solve_opts *o, cudaStream_t st) {
+    const Law<float> law = make_law<float>(*glaw);
+    const int max_outer = o->max_outer > 0 ? o->max_outer : 20;
+    const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-3;
+    std::vector<int> act;
+    for (int i = 0; i < n; ++i)
+        if (items[i].state == 0) act.push_back(i);
+    if (act.empty()) return GBS_OK;
+    // ---- FP64 residuals of every active item, one sync ------------------------------------
+    void *hp = thread_pinned();
+    if (!hp) return set_error(GBS_ECUDA, "no pinned staging buffer");
+    const size_t per = sizeof(OuterScalars);
+    for (size_t k = 0; k < act.size(); k += 4096 / per) {
+        const size_t m = std::min(act.size() - k, (size_t)(4096 / per));
+        for (size_t j = 0; j < m; ++j) {
+            gbsimp_batch_item &it = items[act[k + j]];
+            const int64_t nd = n_dof_of(it.nx, it.ny, it.nz);
+            SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
+            if (it.stats.outer == 0) GBS_CUDA_TRY(cudaMemsetAsync(w.os, 0, sizeof(OuterScalars), st));
+            int rc = ctx->modal_ok ? apply_f64_modal(ctx, it.nx, it.ny, it.nz, glaw, it.x, it.u, w.r64, it.node_mask,
+                                                     w.elem, st)
+                                   : apply_f64(ctx, it.nx, it.ny, it.nz, glaw, it.x, it.u, w.r64, it.node_mask, st);
+            if (rc) return rc;
+            resid64_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, it.f, w.r64, it.node_mask, w.r64, w.partials, w.os);
+            GBS_LAUNCH_CHECK("resid64_kernel");
+            GBS_CUDA_TRY(cudaMemcpyAsync((char *)hp + j * per, w.os, per, cudaMemcpyDeviceToHost, st));
+        }
+        GBS_CUDA_TRY(cudaStreamSynchronize(st));
+        for (size_t j = 0; j < m; ++j) {
+            gbsimp_batch_item &it = items[act[k + j]];
+            OuterScalars h;
+            memcpy(&h, (char *)hp + j * per, per);
+            gbsimp_solve_stats &s = it.stats;
+            s.outer += 1;
+            if (!isfinite(h.rr) || !isfinite(h.ff)) {
+                s.status = GBS_ENONFINITE;
+                it.state = 2;
+            } else if (h.ff == 0.0) {
+                GBS_CUDA_TRY(cudaMemsetAsync(it.u, 0, n_dof_of(it.nx, it.ny, it.nz) * sizeof(double), st));
+                s.relres = 0.0;
+                s.status = GBS_OK;
+                it.state = 1;
+            } else {
+                s.relres = sqrt(h.rr / h.ff);
+                if (s.relres <= o->rtol) {
+                    s.status = GBS_OK;
+                    it.state = 1;
+                } else if (s.outer > max_outer || s.iterations >= o->max_iter) {
+                    s.status = GBS_ENOTCONV;
+                    it.state = 2;
+                }
+            }
+        }
+    }
+    // ---- inner FP32 PCG of the items still above rtol ---------------------------------------
+    std::vector<int> inn;
+    for (int i : act)
+        if (items[i].state == 0) inn.push_back(i);
+    if (inn.empty()) return GBS_OK;
+    for (int i : inn) {
+        gbsimp_batch_item &it = items[i];
+        const int64_t nd = n_dof_of(it.nx, it.ny, it.nz);
+        SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
+        scale_to_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.r64, w.os, w.b32, w.d32);
+        GBS_LAUNCH_CHECK("scale_to_f32_kernel");
+        double itol = o->rtol / it.stats.relres;
+        if (itol < inner) itol = inner;
+        PcgWs pw = pcg_ws(w.pcg, it.nx, it.ny, it.nz);
+        int rc = pcg_setup(ctx, it.nx, it.ny, it.nz, glaw, it.x, w.b32, it.node_mask, w.d32, itol,
+                           o->max_iter - it.stats.iterations, pw, st);
+        if (rc) return rc;
+    }
+    // persistent batched launches (fall back to each item's graph loop)
+    std::vector<int> pending;
+    for (size_t k = 0; k < inn.size(); k += kMaxFused) {
+        const size_t m = std::min(inn.size() - k, (size_t)kMaxFused);
+        FusedItem fi[kMaxFused];
+        for (size_t j = 0; j < m; ++j) {
+            gbsimp_batch_item &it = items[inn[k + j]];
+            SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
+            fi[j] = FusedItem{it.nx, it.ny, it.nz, it.x, it.node_mask, w.d32, pcg_ws(w.pcg, it.nx, it.ny, it.nz)};
+        }
+        if (!o->fused || pcg_fused_batch(ctx, fi, (int)m, law, st) != GBS_OK)
+            for (size_t j = 0; j < m; ++j) pending.push_back(inn[k + j]);
+    }
+    for (int i : pending) {
+        gbsimp_batch_item &it = items[i];
+        SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
+        PcgWs pw = pcg_ws(w.pcg, it.nx, it.ny, it.nz);
+        cudaGraphExec_t exec = nullptr;
+        int rc = loop_graph(ctx, it.nx, it.ny, it.nz, law, it.x, it.node_mask, w.d32, pw, &exec);
+        if (rc) return rc;
+        GBS_CUDA_TRY(cudaGraphLaunch(exec, st));
+    }
+    // finalize, read every item's PCG scalars (one sync), correct u
+    const size_t ps = sizeof(PcgScalars);
+    for (size_t k = 0; k < inn.size(); k += 4096 / ps) {
+        const size_t m = std::min(inn.size() - k, (size_t)(4096 / ps));
+        for (size_t j = 0; j < m; ++j) {
+            gbsimp_batch_item &it = items[inn[k + j]];
+            const int64_t nd = n_dof_of(it.nx, it.ny, it.nz);
+            SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
+            PcgWs pw = pcg_ws(w.pcg, it.nx, it.ny, it.nz);
+            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, pw.p0, pw.p1, w.d32, pw.sc);
+            GBS_LAUNCH_CHECK("pcg_finalize_kernel");
+            GBS_CUDA_TRY(cudaMemcpyAsync((char *)hp + j * ps, pw.sc, ps, cudaMemcpyDeviceToHost, st));
+        }
+        GBS_CUDA_TRY(cudaStreamSynchronize(st));
+        for (size_t j = 0; j < m; ++j) {
+            gbsimp_batch_item &it = items[inn[k + j]];
+            PcgScalars h;
+            memcpy(&h, (char *)hp + j * ps, ps);
+            if (std::find(pending.begin(), pending.end(), inn[k + j]) != pending.end())
+                count_launches(h.trips * (2 * kLoopUnroll + 1));
+            it.stats.iterations += h.iter;
+            if (h.status == GBS_EBREAKDOWN || h.status == GBS_ENONFINITE || h.status == GBS_ETIMEOUT) {
+                it.stats.status = h.status;
+                if (h.iter == 0 || h.status == GBS_ETIMEOUT) {
+                    it.state = 2;
+                    continue;
+                }
+            }
+            const int64_t nd = n_dof_of(it.nx, it.ny, it.nz);
+            SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
+            correct64_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.d32, w.os, it.node_mask, it.u);
+            GBS_LAUNCH_CHECK("correct64_kernel");
+            if (it.stats.status != GBS_OK) it.state = 2;
+        }
+    }
+    return GBS_OK;
+}
+
+}  // namespace gbs
+
+static int check_batch(gbsimp_ctx *ctx, gbsimp_batch_item *items, int n, const gbsimp_law *law,
+                       const gbsimp_solve_opts *opts) {
+    if (!ctx || !law || !opts || n < 0 || (n > 0 && !items)) return set_error(GBS_EINVAL, "gbsimp_batch: bad arguments");
+    for (int i = 0; i < n; ++i) {
+        const gbsimp_batch_item &it = items[i];
+        if (it.state != 0) continue;
+        if (!it.x || !it.f || !it.u || !it.ws || !grid_ok(it.nx, it.ny, it.nz))
+            return set_error(GBS_EINVAL, "gbsimp_batch: item %d has bad arguments", i);
+        if (it.ws_bytes < solve_ws_bytes_impl(it.nx, it.ny, it.nz))
+            return set_error(GBS_EINVAL, "gbsimp_batch: item %d workspace too small", i);
+    }
+    return GBS_OK;
+}
+
+extern "C" int gbsimp_batch_round(gbsimp_ctx *ctx, gbsimp_batch_item *items, int n, const gbsimp_law *law,
+                                  const gbsimp_solve_opts *opts, void *stream) {
+    int rc = check_batch(ctx, items, n, law, opts);
+    if (rc) return rc;
+    return batch_round_impl(ctx, items, n, law, opts, (cudaStream_t)stream);
+}
+
+extern "C" int gbsimp_batch_solve(gbsimp_ctx *ctx, gbsimp_batch_item *items, int n, const gbsimp_law *law,
+                                  const gbsimp_solve_opts *opts, void *stream) {
+    int rc = check_batch(ctx, items, n, law, opts);
+    if (rc) return rc;
+    const int max_rounds = (opts->max_outer > 0 ? opts->max_outer : 20) + 2;
+    for (int r = 0; r < max_rounds; ++r) {
+        bool any = false;
+        for (int i = 0; i < n; ++i) any = any || items[i].state == 0;
+        if (!any) break;
+        rc = batch_round_impl(ctx, items, n, law, opts, (cudaStream_t)stream);
+        if (rc) return rc;
+    }
+    for (int i = 0; i < n; ++i)
+        if (items[i].state == 0) {
+            items[i].state = 2;
+            items[i].stats.status = GBS_ENOTCONV;
+        }
     return GBS_OK;
 }

@@ -214,6 +214,37 @@ int gbsimp_solve(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
                  const float *x, const double *f, const uint8_t *node_mask, double *u,
                  const gbsimp_solve_opts *opts, gbsimp_solve_stats *stats, void *ws,
                  size_t ws_bytes, void *stream);
+/* ---- batched solves (many designs of different sizes in one launch) ------------------ */
+/* One design of a batch. The caller fills the grid, the arrays (same meaning as in
+ * gbsimp_solve) and a workspace of gbsimp_solve_ws_bytes(nx, ny, nz) bytes, sets state = 0
+ * and zeroes stats; the library updates state (0 active, 1 converged, 2 stopped: see
+ * stats.status) and accumulates stats across rounds. */
+typedef struct gbsimp_batch_item {
+    int32_t nx, ny, nz;
+    int32_t state;
+    const float *x;
+    const double *f;
+    const uint8_t *node_mask;
+    double *u;
+    void *ws;
+    size_t ws_bytes;
+    gbsimp_solve_stats stats;
+} gbsimp_batch_item;
+
+/* One round of the FP64 defect correction for every active item: FP64 residuals (one sync
+ * for all), then ONE cooperative launch of a persistent kernel that iterates the FP32 PCG of
+ * every item still above rtol (each item on its own share of the SMs, with its own grid
+ * barrier and scalars, converging independently; up to 24 items per launch), then the FP64
+ * corrections. Items may be added (state 0) or dropped between rounds: the serving loop's
+ * continuous batching. Replaces one gbsimp_solve per design (the reference's one solve per
+ * GPUVoxelFEM.solve, gpu_fem_solver.py:76-133, fed by evaluate_batch's thread pool,
+ * voxel_fem.py:559-611). Synchronises the stream. */
+int gbsimp_batch_round(gbsimp_ctx *ctx, gbsimp_batch_item *items, int n, const gbsimp_law *law,
+                       const gbsimp_solve_opts *opts, void *stream);
+/* Rounds until every item has state != 0. */
+int gbsimp_batch_solve(gbsimp_ctx *ctx, gbsimp_batch_item *items, int n, const gbsimp_law *law,
+                       const gbsimp_solve_opts *opts, void *stream);
+
 /* Jacobi-PCG on a CSR matrix (int32 row_ptr/col_idx, FP32 values, FP32 diagonal), the
  * contract of cuda_kernels.pcg_solve_cuda (cuda_kernels/__init__.py:443-473,
  * simp_pcg_cuda.cu:66-124): x holds x0 on entry; fixed is a list of n_fixed DOF indices

@@ -1,0 +1,65 @@
+"""Batched solves and the serving loop: every result equals the same solve done alone."""
+import numpy as np
+import pytest
+import torch
+
+from genpipeline_gb300 import _lib as L
+from genpipeline_gb300 import designs as D
+from genpipeline_gb300.batch import BatchFEM, FEMDesign, solve_plain
+from genpipeline_gb300.engine import Engine
+from genpipeline_gb300.serve import FEMServer, request_stream
+
+pytestmark = pytest.mark.gpu
+
+# Every design is solved to ||D(f - K u)|| <= 1e-8 ||D f|| (FP64 residual) on both paths, so
+# displacements agree to ~1e-6 of their maximum and compliances to ~1e-7 relative.
+U_TOL, C_TOL = 1e-6, 1e-7
+
+
+def _designs():
+    out = []
+    for k, (grid, load) in enumerate([((24, 24, 24), "cantilever"), ((32, 32, 32), "top_patch"),
+                                      ((40, 20, 20), "cantilever"), ((16, 16, 16), "torsion"),
+                                      ((48, 24, 12), "cantilever")]):
+        if load == "cantilever":
+            from genpipeline_gb300 import bcs
+            f, fixed = bcs.cantilever_tip(*grid)
+        else:
+            f, fixed = D.load_case(load, grid[0])
+        out.append(FEMDesign(grid, D.grf_density(grid, 100 + k), f, fixed))
+    return out
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_batch_equals_single_solves(fused):
+    eng = Engine()
+    single = solve_plain(_designs(), eng)
+    batch = BatchFEM(eng, fused=fused).solve_all(_designs())
+    assert len(batch) == len(single)
+    by_grid = {d.grid: d for d in batch}
+    for s in single:
+        b = by_grid[s.grid]
+        assert b.stats["status"] == L.GBS_OK and b.stats["relres"] <= 1e-8, b.stats
+        us, ub = s.du.cpu().numpy(), b.du.cpu().numpy()
+        np.testing.assert_allclose(ub, us, rtol=0, atol=U_TOL * np.abs(us).max())
+        assert b.compliance == pytest.approx(s.compliance, rel=C_TOL)
+
+
+def test_serving_results_equal_alone_and_in_the_mix():
+    eng = Engine()
+    reqs = request_stream(40, rate=2000.0, edges=(16, 24, 32), repeat_frac=0.15, seed=7)
+    srv = FEMServer(eng, max_slots=8, keep_solutions=True)
+    summary = srv.run(reqs, realtime=True)
+    assert summary["requests"] == 40 and summary["failed"] == 0
+    assert summary["max_active"] > 1  # requests overlapped on the device
+    assert summary["warm_starts"] >= 1
+    for r in reqs:
+        grid = (r.n, r.n, r.n)
+        f, fixed = D.load_case(r.load, r.n)
+        alone = solve_plain([FEMDesign(grid, D.grf_density(grid, r.seed), f, fixed)], eng)[0]
+        assert r.compliance == pytest.approx(alone.compliance, rel=C_TOL), r
+        ua = alone.du.cpu().numpy()
+        np.testing.assert_allclose(r.u.cpu().numpy(), ua, rtol=0, atol=U_TOL * np.abs(ua).max())
+    warm = [r for r in reqs if r.warm]
+    cold = {(r.n, r.seed, r.load): r.iterations for r in reqs if not r.warm}
+    assert all(r.iterations <= cold[(r.n, r.seed, r.load)] for r in warm)
