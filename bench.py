@@ -167,9 +167,12 @@ def _measured_peak():
         return 6800.0, "fallback"
 
 
-def _profiled_traffic():
-    """dram bytes per launch of the PCG apply kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "apply_pcg__simp_64cube.md")
+def _profiled_traffic(workload="simp64"):
+    """dram bytes per launch of the PCG apply kernel from the committed ncu summary of the workload."""
+    name = {"simp64": "apply_pcg__simp_64cube.md", "c4": "apply_pcg__simp_192x96x96.md"}.get(workload)
+    if name is None:
+        return None
+    path = os.path.join(ROOT, "profiles", name)
     try:
         txt = open(path).read()
     except OSError:
@@ -360,7 +363,7 @@ def run_ours(a):
     path = prob.eng.apply_path(GRID[2])
     roof = {"bound": "hbm", "kernel": f"apply_{path}_kernel<PCG> (K(x)p fused with p = z + beta p, x update, p.Ap)",
             "achieved": achieved, "peak": peak, "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": _profiled_traffic(), "alg_bytes_per_launch": alg_bytes, "launch_us": per_launch * 1e6,
+            "traffic": _profiled_traffic(a.workload), "alg_bytes_per_launch": alg_bytes, "launch_us": per_launch * 1e6,
             "fp32_flops_per_launch_dense_equiv": 1152 * ne,
             "est_share_of_step": pcg_iters * per_launch / t}
 

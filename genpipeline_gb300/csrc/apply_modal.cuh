@@ -370,7 +370,9 @@ inline ModalGeom modal_geom(int nx, int ny, int nz, int num_sms, int blocks_per_
     const int S = (ny + 1) * (nz + 1);
     const int tiles = (S + F - 1) / F;
     const int target = (num_sms > 0 ? num_sms : 148) * (blocks_per_sm > 0 ? blocks_per_sm : 1);
-    int nseg = (target + tiles - 1) / tiles;
+    // As many x segments as fit in one wave of resident CTAs (rounding down, so that the
+    // re-rounded segment count never exceeds the target).
+    int nseg = target / tiles;
     if (nseg > nx + 1) nseg = nx + 1;
     if (nseg < 1) nseg = 1;
     const int seglen = (nx + 1 + nseg - 1) / nseg;
