@@ -21,7 +21,7 @@ int launch_apply_plain(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<
 int apply_f32(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
               const float *p, float *y, const uint8_t *mask, cudaStream_t st) {
     if (ctx->modal_ok && modal_fits(nz))
-        return launch_modal<MODE_PLAIN>(ctx, nx, ny, nz, make_law<float>(*law), x, p, y, mask, PcgArgs{}, st);
+        return launch_modal<MODE_PLAIN>(ctx, nx, ny, nz, make_law<float>(*law), x, p, y, mask, CgArgs{}, st);
     return launch_apply_plain<TileF, float, KeF>(ctx, nx, ny, nz, make_law<float>(*law), ctx->kef, x, p, y, mask,
                                                  st);
 }

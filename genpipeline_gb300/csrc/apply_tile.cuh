@@ -20,9 +20,11 @@
 
 namespace gbs {
 
-// MODE_FUSED: the PCG pass inside the persistent kernel; vectors that other CTAs rewrite
-// between passes are read at L2 (L1 is not coherent across SMs within one launch).
-enum { MODE_PLAIN = 0, MODE_PCG = 1, MODE_FUSED = 2 };
+// MODE_PCG: K1 of the two-kernel PCG iteration (dense kernel). MODE_CG: the one-kernel
+// single-reduction PCG iteration (modal kernel); MODE_CG_FUSED: the same pass inside the
+// persistent kernel, where vectors that other CTAs rewrite between passes are read at L2
+// (L1 is not coherent across SMs within one launch).
+enum { MODE_PLAIN = 0, MODE_PCG = 1, MODE_CG = 3, MODE_CG_FUSED = 4 };
 
 // Device-resident state of one Jacobi-PCG solve (FP32 vectors, FP64 scalars).
 struct PcgScalars {
@@ -41,7 +43,7 @@ struct PcgScalars {
     unsigned bar_count, bar_gen;  // grid barrier of the persistent kernel
     int trips;        // WHILE-loop trips run by the device-driven loop
     int max_trips;    // hard cap on those trips (the loop always ends)
-    int pad;
+    int freeze;       // 1 = kernels leave the scalars as they are (timing of one pass)
 };
 
 struct PcgArgs {
@@ -52,6 +54,19 @@ struct PcgArgs {
     float *xu;          // iterate; K1 of step k adds alpha_{k-1} p_{k-1}
     double *partials;   // one double per block
     PcgScalars *sc;
+};
+
+// Buffers of the single-reduction PCG (MODE_CG). Iteration i reads r[i&1], w[i&1],
+// s[(i+1)&1] and writes r[(i+1)&1], w[(i+1)&1], s[i&1]; p and x are updated in place.
+struct CgArgs {
+    float *r[2];        // r_i (masked residual)
+    float *w[2];        // w_i = D K D u_i, u_i = M r_i
+    float *s[2];        // s_i = D K D p_i
+    float *p;           // search direction
+    float *xu;          // iterate
+    const float *dinv;  // M = 1/diag(K) on free DOFs, 0 on fixed DOFs
+    double *partials;   // three doubles per block
+    PcgScalars *sc;     // alpha[0] = alpha_i, beta = beta_i, rz = gamma_i = r_i.u_i
 };
 
 template <typename T>

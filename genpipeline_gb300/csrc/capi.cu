@@ -138,9 +138,17 @@ static void install_ke(gbsimp_ctx *ctx, const double *ke) {
                 kmax = fmax(kmax, fabs(km[r][cc]));
             }
         bool in_pattern[24][24] = {};
+        int cls_first[kModalClasses];
+        for (int k = kModalClasses - 1; k >= 0; --k)
+            for (int i = kModalNnz - 1; i >= 0; --i)
+                if (modal_class(i) == k) cls_first[k] = i;
+        bool classes_ok = true;
         for (int i = 0; i < kModalNnz; ++i) {
             in_pattern[modal_row(i)][modal_col(i)] = true;
-            ctx->km.v[i] = (float)km[modal_row(i)][modal_col(i)];
+            const double kc = km[modal_row(cls_first[modal_class(i)])][modal_col(cls_first[modal_class(i)])];
+            if (fabs(km[modal_row(i)][modal_col(i)] - kc) > 1e-9 * kmax) classes_ok = false;
+            const float kf = (float)kc;
+            ctx->km.c[modal_class(i)] = make_float2(kf, kf);
             ctx->kmd.v[i] = km[modal_row(i)][modal_col(i)];
         }
         bool ok = kmax > 0.0;
@@ -150,7 +158,7 @@ static void install_ke(gbsimp_ctx *ctx, const double *ke) {
                     ok = false;
                     break;
                 }
-        ctx->modal_ok = ok;
+        ctx->modal_ok = ok && classes_ok;
     }
     for (int i = 0; i < 24; ++i) {
         ctx->ke_diag_d[i] = ke[i * 25];
@@ -186,6 +194,8 @@ extern "C" int gbsimp_create(gbsimp_ctx **out) {
         return cuda_error(e, "cudaGetDevice");
     }
     e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&c->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
     if (e != cudaSuccess) {
         free(c);
         return cuda_error(e, "cudaDeviceGetAttribute");

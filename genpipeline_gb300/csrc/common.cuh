@@ -136,8 +136,44 @@ __host__ __device__ constexpr int modal_col(int i) {
     return c[i];
 }
 
+// Km splits into 11 independent blocks of 1-3 (mode, component) indices; row r only reads
+// columns of its own block, so r = Km q can overwrite q block by block.
+constexpr int kModalBlocks = 11;
+__host__ __device__ constexpr int modal_block(int b, int a) {
+    constexpr int m[kModalBlocks][3] = {{3, 14, -1},  {4, 8, -1},   {5, 7, 12},   {6, 13, -1},
+                                        {9, 16, 20},  {10, 15, -1}, {11, 18, -1}, {17, 19, -1},
+                                        {21, -1, -1}, {22, -1, -1}, {23, -1, -1}};
+    return m[b][a];
+}
+__host__ __device__ constexpr int modal_block_of(int r) {
+    for (int b = 0; b < kModalBlocks; ++b)
+        for (int a = 0; a < 3; ++a)
+            if (modal_block(b, a) == r) return b;
+    return -1;
+}
+__host__ __device__ constexpr bool modal_blocks_closed() {
+    for (int i = 0; i < kModalNnz; ++i)
+        if (modal_block_of(modal_row(i)) < 0 || modal_block_of(modal_row(i)) != modal_block_of(modal_col(i)))
+            return false;
+    return true;
+}
+static_assert(modal_blocks_closed(), "every Km entry must lie inside one block");
+__host__ __device__ constexpr bool modal_row_first(int i) { return i == 0 || modal_row(i - 1) != modal_row(i); }
+
+// By the cube's symmetry the 45 coefficients take at most 8 distinct values for any isotropic
+// material (fewer for some Poisson ratios, e.g. 7 at nu = 0.3); entry i has the value of class
+// modal_class(i). capi.cu checks this for the installed Ke.
+constexpr int kModalClasses = 8;
+__host__ __device__ constexpr int modal_class(int i) {
+    constexpr int k[kModalNnz] = {0, 0, 0, 0, 1, 2, 2, 0, 0, 2, 1, 2, 0, 0, 3, 4, 4, 5, 6, 5, 6, 2, 2,
+                                  1, 0, 0, 0, 0, 6, 5, 4, 3, 4, 5, 6, 6, 5, 6, 5, 4, 4, 3, 7, 7, 7};
+    return k[i];
+}
+
+// The class values, each duplicated into both lanes of a float2 (packed FP32x2 operands: one
+// thread works on two elements at once).
 struct ModalK {
-    float v[kModalNnz];
+    float2 c[kModalClasses];
 };
 struct ModalKD {
     double v[kModalNnz];
@@ -155,6 +191,7 @@ struct gbsimp_ctx {
     float ke_diag_f[24];
     double ke_diag_d[24];
     int num_sms;
+    int smem_per_sm;        // shared memory per SM (bytes)
     bool modal_ok;          // Ke has the modal sparsity of an isotropic cube element
     gbs::ModalK km;         // its 45 modal coefficients (Km / 64)
     gbs::ModalKD kmd;       // the same in FP64

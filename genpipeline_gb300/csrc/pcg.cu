@@ -1,11 +1,17 @@
 // pcg.cu -- Jacobi-PCG drivers: FP32 matrix-free PCG, FP32-inner / FP64-outer defect
 // correction, and a CSR PCG for the pcg_solve_cuda contract.
 //
-// One PCG iteration k is two launches (after setup r_0, z_0 = r_0/diag, p_{-1} = 0):
+// Two forms of the same Jacobi-PCG (simp_solver_gpu.py:328-379: z = r/diag, stop when
+// ||r|| < rtol ||D b||):
+// - modal element (isotropic cube Ke): one launch per iteration, the single-reduction form
+//   (apply_modal.cuh, MODE_CG): the staging of the apply operand u_{i+1} = M r_{i+1} also
+//   forms s_i and r_{i+1}, the owned nodes update p and x, and the block sums of r.u, w.u and
+//   r.r give beta_{i+1} and alpha_{i+1} in the last block. Setup: r_0, u_0, w_0 = A u_0,
+//   alpha_0 = (r_0.u_0) / (w_0.u_0).
+// - dense element (any other Ke): two launches per iteration k (setup r_0, p_{-1} = 0):
 //   K1  apply_tile_kernel<MODE_PCG>: p_k = z_k + beta_k p_{k-1} on the halo while staging,
 //       x += alpha_{k-1} p_{k-1} on owned nodes, Ap_k = D K D p_k, p_k.Ap_k -> alpha_k.
-//   K2  pcg_update_kernel: r_{k+1} = r_k - alpha_k Ap_k, ||r||^2 and r.z -> beta_{k+1},
-//       the stop test ||r|| < rtol ||D b|| (simp_solver_gpu.py:328-379).
+//   K2  pcg_update_kernel: r_{k+1} = r_k - alpha_k Ap_k, ||r||^2 and r.z -> beta_{k+1}.
 // Every scalar lives on the device; each kernel exits at once when the solve is done, so
 // the host can launch whole chunks of iterations and look at the status once per chunk.
 #include <math.h>
@@ -35,12 +41,16 @@ static inline unsigned vec_blocks(const gbsimp_ctx *ctx, int64_t n) {
 }
 
 // ---- workspace of the FP32 PCG -----------------------------------------------------------
+// Dense form: r, dinv, p0/p1 (p_k in p[k&1]), ap. Single-reduction form: r/r1 (r[i&1]),
+// ap/p1 (w[i&1]), s0/s1 (s[i&1]), p0 (p), dinv.
 struct PcgWs {
     PcgScalars *sc;
-    float *r, *dinv, *p0, *p1, *ap;
+    float *r, *dinv, *p0, *p1, *ap, *r1, *s0, *s1;
     double *partials;
     size_t partial_count;
 };
+
+static inline bool use_modal(const gbsimp_ctx *ctx, int nz) { return ctx->modal_ok && modal_fits(nz); }
 
 static size_t pcg_partials(int nx, int ny, int nz) {
     const dim3 g = tile_grid<TileF>(nx, ny, nz);
@@ -50,7 +60,7 @@ static size_t pcg_partials(int nx, int ny, int nz) {
 
 static size_t pcg_ws_bytes_impl(int nx, int ny, int nz) {
     const size_t nd = (size_t)n_dof_of(nx, ny, nz);
-    return al256(sizeof(PcgScalars)) + 5 * al256(nd * sizeof(float)) + al256(pcg_partials(nx, ny, nz) * sizeof(double));
+    return al256(sizeof(PcgScalars)) + 8 * al256(nd * sizeof(float)) + al256(pcg_partials(nx, ny, nz) * sizeof(double));
 }
 
 static PcgWs pcg_ws(void *ws, int nx, int ny, int nz) {
@@ -59,14 +69,30 @@ static PcgWs pcg_ws(void *ws, int nx, int ny, int nz) {
     PcgWs w;
     w.sc = (PcgScalars *)p;
     p += al256(sizeof(PcgScalars));
-    float **v[5] = {&w.r, &w.dinv, &w.p0, &w.p1, &w.ap};
-    for (int i = 0; i < 5; ++i) {
+    float **v[8] = {&w.r, &w.dinv, &w.p0, &w.p1, &w.ap, &w.r1, &w.s0, &w.s1};
+    for (int i = 0; i < 8; ++i) {
         *v[i] = (float *)p;
         p += al256(nd * sizeof(float));
     }
     w.partials = (double *)p;
     w.partial_count = pcg_partials(nx, ny, nz);
     return w;
+}
+
+static CgArgs cg_args(const PcgWs &w, float *u) {
+    CgArgs a;
+    a.r[0] = w.r;
+    a.r[1] = w.r1;
+    a.w[0] = w.ap;
+    a.w[1] = w.p1;
+    a.s[0] = w.s0;
+    a.s[1] = w.s1;
+    a.p = w.p0;
+    a.xu = u;
+    a.dinv = w.dinv;
+    a.partials = w.partials;
+    a.sc = w.sc;
+    return a;
 }
 
 __device__ __forceinline__ bool dof_fixed(const uint8_t *mask, int64_t d) {
@@ -163,6 +189,73 @@ __global__ void pcg_init_kernel(int64_t nd, const float *__restrict__ b, const f
     }
 }
 
+// Single-reduction setup, step 1: r_0 = D b - q (q = D K D x0, read from `qu`), u_0 = M r_0
+// written over q, p_{-1} = s_{-1} = 0, fixed entries of x0 zeroed; sums r.u, r.r, (Db).(Db)
+// and the stop test of the initial guess.
+__global__ void cg_init_kernel(int64_t nd, const float *__restrict__ b, float *qu, const uint8_t *__restrict__ mask,
+                               const float *__restrict__ dinv, float *r, float *p, float *sprev, float *xu,
+                               double *partials, PcgScalars *sc, double tol, int max_iter, int max_trips) {
+    float ru = 0.0f, rr = 0.0f, bb = 0.0f;
+    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
+        const bool fx = dof_fixed(mask, d);
+        const float bd = fx ? 0.0f : b[d];
+        const float rd = fx ? 0.0f : bd - qu[d];
+        const float ud = dinv[d] * rd;
+        r[d] = rd;
+        qu[d] = ud;
+        p[d] = 0.0f;
+        sprev[d] = 0.0f;
+        if (fx) xu[d] = 0.0f;
+        ru = fmaf(rd, ud, ru);
+        rr = fmaf(rd, rd, rr);
+        bb = fmaf(bd, bd, bb);
+    }
+    __shared__ double tot[3];
+    if (last_block3(ru, rr, bb, partials, &sc->counter, tot) && threadIdx.x == 0) {
+        sc->rz = tot[0];
+        sc->rr = tot[1];
+        sc->bnorm = sqrt(tot[2]);
+        sc->alpha[0] = sc->alpha[1] = 0.0;
+        sc->beta = 0.0;
+        sc->tol = tol;
+        sc->pap = 0.0;
+        sc->iter = 0;
+        sc->max_iter = max_iter;
+        sc->trips = 0;
+        sc->max_trips = max_trips;
+        sc->freeze = 0;
+        sc->status = GBS_OK;
+        const bool fin = isfinite(tot[0]) && isfinite(tot[1]) && isfinite(tot[2]);
+        sc->done = (!fin || sc->bnorm == 0.0 || sqrt(tot[1]) < tol * sc->bnorm || max_iter <= 0) ? 1 : 0;
+        if (!fin) sc->status = GBS_ENONFINITE;
+        else if (max_iter <= 0 && !(sqrt(tot[1]) < tol * sc->bnorm) && sc->bnorm != 0.0) sc->status = GBS_ENOTCONV;
+    }
+}
+
+// Single-reduction setup, step 2 (after w_0 = D K D u_0): alpha_0 = (r_0.u_0) / (w_0.u_0),
+// beta_0 = 0.
+__global__ void cg_start_kernel(int64_t nd, const float *__restrict__ w, const float *__restrict__ u,
+                                double *partials, PcgScalars *sc) {
+    if (sc->done) return;
+    float wu = 0.0f;
+    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x)
+        wu = fmaf(w[d], u[d], wu);
+    __shared__ double tot[3];
+    if (last_block3(wu, 0.0, 0.0, partials, &sc->counter, tot) && threadIdx.x == 0) {
+        sc->pap = tot[0];
+        if (!isfinite(tot[0])) {
+            sc->done = 1;
+            sc->status = GBS_ENONFINITE;
+        } else if (!(tot[0] > 0.0)) {
+            sc->done = 1;
+            sc->status = GBS_EBREAKDOWN;
+        } else {
+            sc->alpha[0] = sc->rz / tot[0];
+            sc->beta = 0.0;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256) pcg_update_kernel(int64_t nd, const float *__restrict__ ap,
                                                          const float *__restrict__ dinv, float *r, double *partials,
                                                          PcgScalars *sc) {
@@ -194,13 +287,15 @@ __global__ void __launch_bounds__(256) pcg_update_kernel(int64_t nd, const float
     }
 }
 
-// x += alpha_last p_last after the loop (the iteration that met the stop test has not yet
-// added its own step), or x = 0 when D b = 0.
-__global__ void pcg_finalize_kernel(int64_t nd, const float *p0, const float *p1, float *xu, const PcgScalars *sc) {
+// After the loop: x = 0 when D b = 0; otherwise the dense form (lazy = 1) adds alpha_last
+// p_last (the iteration that met the stop test has not yet added its own step). The
+// single-reduction form has x complete already.
+__global__ void pcg_finalize_kernel(int64_t nd, const float *p0, const float *p1, float *xu, const PcgScalars *sc,
+                                    int lazy) {
     const int st = sc->status;
     const int it = sc->iter;
     const bool zero = sc->bnorm == 0.0;
-    if (!zero && (it == 0 || st == GBS_EBREAKDOWN || st == GBS_ENONFINITE)) return;
+    if (!zero && (!lazy || it == 0 || st == GBS_EBREAKDOWN || st == GBS_ENONFINITE)) return;
     const float alpha = (float)sc->alpha[(it - 1) & 1];
     const float *p = ((it - 1) & 1) ? p1 : p0;
     for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x)
@@ -216,14 +311,17 @@ static int read_scalars(const PcgScalars *d, PcgScalars *h, cudaStream_t st) {
     return GBS_OK;
 }
 
-// Launches one K1+K2 iteration.
+// Launches one iteration: the single-reduction kernel (modal element) or K1 + K2.
 static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
                          const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st, cudaEvent_t after_k1) {
-    PcgArgs pa{w.r, w.dinv, w.p0, w.p1, u, w.partials, w.sc};
-    if (ctx->modal_ok && modal_fits(nz)) {
-        int rc = launch_modal<MODE_PCG>(ctx, nx, ny, nz, law, x, nullptr, w.ap, mask, pa, st);
+    if (use_modal(ctx, nz)) {
+        int rc = launch_modal<MODE_CG>(ctx, nx, ny, nz, law, x, nullptr, nullptr, mask, cg_args(w, u), st);
         if (rc) return rc;
-    } else {
+        if (after_k1) GBS_CUDA_TRY(cudaEventRecord(after_k1, st));
+        return GBS_OK;
+    }
+    PcgArgs pa{w.r, w.dinv, w.p0, w.p1, u, w.partials, w.sc};
+    {
         TileArgs<float> A{nx, ny, nz, x, nullptr, w.ap, mask};
         const dim3 g = tile_grid<TileF>(nx, ny, nz), b = tile_block<TileF>();
         if (ctx->translation_free)
@@ -242,11 +340,11 @@ static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const La
 // FP32 PCG. u: x0 in, solution out. Returns GBS_OK and fills *out (status inside).
 // ---- persistent fused PCG: the whole solve in one cooperative launch ---------------------
 // Every CTA keeps its (flat tile, x segment) of the modal apply for all iterations. One
-// iteration = the PCG apply pass (p = z + beta p, x += alpha p_old, Ap, p.Ap) -> grid
-// barrier that reduces p.Ap to alpha -> r -= alpha Ap on the owned nodes with r.r, r.z ->
-// grid barrier that reduces them to beta and the stop test. The last CTA to arrive at a
-// barrier does the fixed-order reduction and releases the others. Each wait is bounded in
-// time (%globaltimer): on expiry the CTA records GBS_ETIMEOUT, sets done and leaves.
+// iteration = the single-reduction pass (apply_modal.cuh, MODE_CG_FUSED) -> one grid barrier
+// that sums r.u, w.u and r.r -> the scalar step, which every CTA computes from the same
+// totals. The barrier publishes per-block partials and every block sums them in block order
+// (deterministic, no serial finisher). Each wait is bounded in time (%globaltimer): on expiry
+// the CTA records GBS_ETIMEOUT, sets done and leaves.
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -307,8 +405,7 @@ struct FusedDesign {
     int tiles, block0, nblk, pad;
     const float *x;
     const uint8_t *mask;
-    float *ap;
-    PcgArgs pa;
+    CgArgs ca;
 };
 struct FusedTable {
     int n, pad;
@@ -325,88 +422,35 @@ __global__ void __launch_bounds__(NT, 2)
     while (di + 1 < T.n && (int)blockIdx.x >= T.d[di + 1].block0) ++di;
     const FusedDesign &D = T.d[di];
     const ModalGeom &G = D.G;
-    const PcgArgs &pa = D.pa;
+    const CgArgs &ca = D.ca;
     const int bid = (int)blockIdx.x - D.block0;
     const int nblk = D.nblk;
     const int tile = bid % D.tiles, seg = bid / D.tiles;
-    PcgScalars *sc = pa.sc;
-    const int nz = G.nz, NZ = nz + 1, S = (G.ny + 1) * NZ;
-    const int F = NT * EPT - (nz + 2);
-    const int F0 = tile * F;
-    const int nf = max(0, min(F, S - F0));
-    const int xs = seg * G.seglen;
-    const int np = max(0, min(xs + G.seglen, G.nx + 1) - xs);
-    const int owned = nf * np;
+    PcgScalars *sc = ca.sc;
     // The solve's scalars, identical in every block of the design (each block computes them).
     const volatile PcgScalars *vsc = sc;
     int it = vsc->iter, done = vsc->done, status = vsc->status;
-    double rz = vsc->rz, beta = vsc->beta, alpha_prev = vsc->alpha[(it + 1) & 1], rr = vsc->rr;
+    double gamma_i = vsc->rz, alpha = vsc->alpha[0], beta = vsc->beta, rr = vsc->rr, delta = vsc->pap;
     const double tol = vsc->tol, bnorm = vsc->bnorm;
     const int max_iter = vsc->max_iter;
     unsigned target = 0;
-    double alpha = 0.0, pap = 0.0;
     while (!done) {
-        PcgPass pp;
-        pp.beta = (float)beta;
-        pp.alpha_prev = (float)alpha_prev;
-        pp.r = pa.r;
-        pp.dinv = pa.dinv;
-        pp.pold = (it & 1) ? pa.pbuf0 : pa.pbuf1;
-        pp.pnew = (it & 1) ? pa.pbuf1 : pa.pbuf0;
-        pp.xu = pa.xu;
-        const double part =
-            modal_pass<NT, EPT, MAXN, MODE_FUSED>(G, D.x, nullptr, D.ap, D.mask, law, km, pp, smem4, tile, seg);
+        const int c = it & 1, nc = c ^ 1;
+        const CgPass cp{(float)alpha, (float)beta, ca.r[c], ca.w[c], ca.s[nc], ca.dinv, ca.r[nc], ca.s[c], ca.p, ca.xu};
+        float sums[3];
+        modal_pass<NT, EPT, MAXN, MODE_CG_FUSED>(G, D.x, nullptr, ca.w[nc], D.mask, law, km, cp, smem4, tile, seg,
+                                                 sums);
         __threadfence();
         target += nblk;
-        double t1[1];
-        const double v1[1] = {part};
-        if (!grid_sums<1>(v1, pa.partials, 0, &sc->bar_count, target, nblk, bid, wait_ns, sred, t1)) {
+        double tot[3];
+        const double v[3] = {(double)sums[0], (double)sums[1], (double)sums[2]};
+        if (!grid_sums<3>(v, ca.partials, it & 1, &sc->bar_count, target, nblk, bid, wait_ns, sred, tot)) {
             status = GBS_ETIMEOUT;
             break;
         }
-        pap = t1[0];
-        if (!(pap > 0.0) || !isfinite(pap)) {
-            status = isfinite(pap) ? GBS_EBREAKDOWN : GBS_ENONFINITE;
-            alpha = 0.0;
-            done = 1;
-            break;
-        }
-        alpha = rz / pap;
-        const float af = (float)alpha;
-        float rzf = 0.0f, rrf = 0.0f;
-        for (int q = threadIdx.x; q < owned; q += NT) {
-            const int64_t n = (int64_t)(xs + q / nf) * S + F0 + q % nf;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const int64_t d = 3 * n + c;
-                const float rd = fmaf(-af, __ldcg(&D.ap[d]), __ldcg(&pa.r[d]));
-                const_cast<float *>(pa.r)[d] = rd;
-                rrf = fmaf(rd, rd, rrf);
-                rzf = fmaf(rd * pa.dinv[d], rd, rzf);
-            }
-        }
-        __threadfence();
-        target += nblk;
-        double t2[2];
-        const double v2[2] = {(double)rzf, (double)rrf};
-        if (!grid_sums<2>(v2, pa.partials, 1, &sc->bar_count, target, nblk, bid, wait_ns, sred, t2)) {
-            status = GBS_ETIMEOUT;
-            break;
-        }
-        it += 1;
-        rr = t2[1];
-        if (!isfinite(t2[0]) || !isfinite(t2[1])) {
-            status = GBS_ENONFINITE;
-            done = 1;
-        } else if (sqrt(t2[1]) < tol * bnorm) {
-            done = 1;
-        } else if (it >= max_iter) {
-            status = GBS_ENOTCONV;
-            done = 1;
-        }
-        beta = t2[0] / rz;
-        rz = t2[0];
-        alpha_prev = alpha;
+        rr = tot[2];
+        delta = tot[1];
+        cg_scalar_step(tot[0], tot[1], tot[2], tol, bnorm, max_iter, it, done, status, gamma_i, alpha, beta);
     }
     if (status == GBS_ETIMEOUT) {
         if (threadIdx.x == 0) {
@@ -419,12 +463,11 @@ __global__ void __launch_bounds__(NT, 2)
         sc->iter = it;
         sc->done = 1;
         sc->status = status;
-        sc->rz = rz;
+        sc->rz = gamma_i;
         sc->rr = rr;
+        sc->pap = delta;
+        sc->alpha[0] = alpha;
         sc->beta = beta;
-        sc->pap = pap;
-        // the finalize kernel adds alpha_last p_last: p_{it-1} lives in buffer (it-1)&1
-        sc->alpha[(it - 1) & 1] = status == GBS_EBREAKDOWN || status == GBS_ENONFINITE ? 0.0 : alpha;
     }
 }
 
@@ -453,20 +496,21 @@ static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n,
     }
     void *kern = small ? (void *)pcg_fused_kernel<kModalNT, kModalEPT, kModalEPT + 1>
                        : (void *)pcg_fused_kernel<kModalNT, kModalEPT, kModalEPT + 2>;
-    static int per_sm_cache[2][128] = {};
+    static int ready_cache[2][128] = {};  // 1 = attribute set and cooperative launch supported, -1 = not
+    static int reg_cache[2][128] = {};
     const int dev = ctx->device >= 0 && ctx->device < 128 ? ctx->device : 0;
-    int &per_sm = per_sm_cache[small ? 0 : 1][dev];
-    const int smax = (int)modal_smem_bytes<kModalNT, kModalEPT>(446);
-    if (per_sm == 0) {
-        int v = 0, coop = 0;
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, kModalNT, smax) != cudaSuccess ||
-            cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
-            v = -1;
+    int &ready = ready_cache[small ? 0 : 1][dev];
+    const size_t smem = modal_smem_bytes<kModalNT, kModalEPT>(max_nz, true);
+    if (ready == 0) {
+        const int smax = (int)modal_smem_bytes<kModalNT, kModalEPT>(446, true);
+        int coop = 0;
+        const bool ok = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) == cudaSuccess &&
+                        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) == cudaSuccess && coop;
         cudaGetLastError();
-        per_sm = v > 0 ? v : -1;
+        ready = ok ? 1 : -1;
     }
-    if (per_sm < 1) return GBS_EINVAL;
+    if (ready < 0) return GBS_EINVAL;
+    const int per_sm = modal_resident(ctx, kern, reg_cache[small ? 0 : 1][dev], smem);
     const int total = per_sm * (ctx->num_sms > 0 ? ctx->num_sms : 148);
     int tiles[kMaxFused], nseg[kMaxFused], seglen[kMaxFused];
     double welem = 0.0;
@@ -511,11 +555,9 @@ static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n,
         D.nblk = tiles[i] * nseg[i];
         D.x = itm.x;
         D.mask = itm.mask;
-        D.ap = itm.w.ap;
-        D.pa = PcgArgs{itm.w.r, itm.w.dinv, itm.w.p0, itm.w.p1, itm.u, itm.w.partials, itm.w.sc};
+        D.ca = cg_args(itm.w, itm.u);
         block0 += D.nblk;
     }
-    const size_t smem = modal_smem_bytes<kModalNT, kModalEPT>(max_nz);
     unsigned long long wait_ns = 2000000000ull;  // 2 s per barrier wait
     Law<float> lw = law;
     ModalK km = ctx->km;
@@ -530,11 +572,16 @@ static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n,
 }
 
 // ---- device-driven PCG loop: one CUDA graph with a WHILE node ------------------------------
-// Body: kLoopUnroll x (K1, K2) and a one-thread kernel that sets the loop condition from
-// the device flag `done`. K1/K2 return at once when done is set, so a finished solve costs
-// at most kLoopUnroll-1 empty iterations. The condition kernel also counts trips and stops
+// Body: kLoopUnroll iterations (one kernel each, or K1 + K2 for the dense element) and a
+// one-thread kernel that sets the loop condition from the device flag `done`. The iteration
+// kernels return at once when done is set, so a finished solve costs at most kLoopUnroll-1
+// empty iterations. The condition kernel also counts trips and stops
 // the loop with GBS_ETIMEOUT after max_trips (set from max_iter), so the loop always ends.
 constexpr int kLoopUnroll = 8;
+
+static inline int launches_per_trip(const gbsimp_ctx *ctx, int nz) {
+    return (use_modal(ctx, nz) ? 1 : 2) * kLoopUnroll + 1;
+}
 
 __global__ void pcg_loop_cond_kernel(cudaGraphConditionalHandle h, PcgScalars *sc) {
     const int trips = sc->trips + 1;
@@ -581,7 +628,7 @@ static int loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<f
                       const uint8_t *mask, float *u, const PcgWs &w, cudaGraphExec_t *out) {
     GraphCache *gc = (GraphCache *)ctx->graphs;
     if (!gc) return set_error(GBS_ECUDA, "no graph cache");
-    const bool modal = ctx->modal_ok && modal_fits(nz);
+    const bool modal = use_modal(ctx, nz);
     LoopKey k;
     memset(&k, 0, sizeof k);
     k.ws = w.sc;
@@ -610,7 +657,7 @@ static int loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<f
         gc->map.clear();
     }
     if (modal) {
-        const int r = modal_prepare<MODE_PCG>(ctx, nz);
+        const int r = modal_prepare<MODE_CG>(ctx, nz);
         if (r < 0) return -r;
     }
     if (!gc->cap) GBS_CUDA_TRY(cudaStreamCreateWithFlags(&gc->cap, cudaStreamNonBlocking));
@@ -670,8 +717,9 @@ static int loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<f
     return GBS_OK;
 }
 
-// PCG setup on the stream: zeroed scalars, 1/diag, q = D K D u, r = D b - q, z, p_{-1} = 0,
-// the first dot products and the stop test (nothing is read back).
+// PCG setup on the stream: zeroed scalars, 1/diag, q = D K D u, r = D b - q, then for the
+// single-reduction form u_0 = M r_0, w_0 = D K D u_0 and alpha_0, for the dense form
+// p_{-1} = 0; the first dot products and the stop test (nothing is read back).
 static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x,
                      const float *b, const uint8_t *mask, float *u, double rtol, int max_iter, const PcgWs &w,
                      cudaStream_t st) {
@@ -680,10 +728,24 @@ static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp
     GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
     dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, law, ctx->kef, x, mask, w.dinv);
     GBS_LAUNCH_CHECK("dinv_kernel");
+    const int max_trips = (max_iter + kLoopUnroll - 1) / kLoopUnroll + 2;
+    if (use_modal(ctx, nz)) {
+        const CgArgs ca = cg_args(w, u);
+        int rc = apply_f32(ctx, nx, ny, nz, glaw, x, u, ca.w[1], mask, st);
+        if (rc) return rc;
+        cg_init_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, b, ca.w[1], mask, w.dinv, ca.r[0], ca.p, ca.s[1], u,
+                                                           w.partials, w.sc, rtol, max_iter, max_trips);
+        GBS_LAUNCH_CHECK("cg_init_kernel");
+        rc = apply_f32(ctx, nx, ny, nz, glaw, x, ca.w[1], ca.w[0], mask, st);
+        if (rc) return rc;
+        cg_start_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, ca.w[0], ca.w[1], w.partials, w.sc);
+        GBS_LAUNCH_CHECK("cg_start_kernel");
+        return GBS_OK;
+    }
     int rc = apply_f32(ctx, nx, ny, nz, glaw, x, u, w.ap, mask, st);
     if (rc) return rc;
     pcg_init_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, b, w.ap, mask, w.dinv, w.r, w.p1, u, w.partials, w.sc, rtol,
-                                                        max_iter, (max_iter + kLoopUnroll - 1) / kLoopUnroll + 2);
+                                                        max_iter, max_trips);
     GBS_LAUNCH_CHECK("pcg_init_kernel");
     return GBS_OK;
 }
@@ -709,7 +771,7 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
     if (!prof && !h.done && fused) {
         const FusedItem item{nx, ny, nz, x, mask, u, w};
         if (pcg_fused_batch(ctx, &item, 1, law, st) == GBS_OK) {
-            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc);
+            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, 0);
             GBS_LAUNCH_CHECK("pcg_finalize_kernel");
             rc = read_scalars(w.sc, &h, st);
             if (rc) return rc;
@@ -722,11 +784,11 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
         cudaGraphExec_t exec = nullptr;
         if (loop_graph(ctx, nx, ny, nz, law, x, mask, u, w, &exec) == GBS_OK) {
             GBS_CUDA_TRY(cudaGraphLaunch(exec, st));
-            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc);
+            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 0 : 1);
             GBS_LAUNCH_CHECK("pcg_finalize_kernel");
             rc = read_scalars(w.sc, &h, st);
             if (rc) return rc;
-            count_launches(h.trips * (2 * kLoopUnroll + 1));
+            count_launches(h.trips * launches_per_trip(ctx, nz));
             *out = h;
             return GBS_OK;
         }
@@ -753,7 +815,8 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
         if (rc) return rc;
         if (prof) {
             int ran = h.iter - it0;
-            if (h.status == GBS_EBREAKDOWN || h.status == GBS_ENONFINITE) ++ran;  // K1 ran, K2 did not
+            // dense form: on breakdown K1 ran without K2
+            if (!use_modal(ctx, nz) && (h.status == GBS_EBREAKDOWN || h.status == GBS_ENONFINITE)) ++ran;
             for (int i = 0; i < ran && i < n; ++i) {
                 float ms = 0.0f;
                 GBS_CUDA_TRY(cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]));
@@ -764,7 +827,7 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
         if (check_every <= 0 && chunk < max_chunk) chunk *= 2;
     }
     for (auto &e : ev) cudaEventDestroy(e);
-    pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc);
+    pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 0 : 1);
     GBS_LAUNCH_CHECK("pcg_finalize_kernel");
     rc = read_scalars(w.sc, &h, st);
     if (rc) return rc;
@@ -1095,6 +1158,8 @@ __global__ void fill_f32_kernel(int64_t n, float v, float *a) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
 }
 
+__global__ void freeze_scalars_kernel(PcgScalars *sc) { sc->freeze = 1; }
+
 extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x,
                                      const uint8_t *node_mask, int reps, void *ws, size_t ws_bytes,
                                      double *seconds_per_launch, void *stream) {
@@ -1107,17 +1172,24 @@ extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, co
     PcgWs w = pcg_ws(ws, nx, ny, nz);
     float *xu = (float *)((char *)ws + pcg_ws_bytes_impl(nx, ny, nz));
     const Law<float> law = make_law<float>(*glaw);
-    // A state on which every K1 launch does full work: r = 1 (p = r/diag > 0 on free DOFs,
-    // so p.Ap > 0), beta = 0, iteration 0 (K2 never runs, so every launch repeats step 0).
+    // A state on which every launch does the full work of one iteration and repeats it:
+    // r = 1, everything else 0 (alpha = beta = 0), iteration 0. Single-reduction kernel: the
+    // scalars are frozen, so no launch advances the iteration. Dense form: K2 never runs.
+    const bool modal = use_modal(ctx, nz);
     GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
     dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, law, ctx->kef, x, node_mask, w.dinv);
     fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 1.0f, w.r);
     fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.p1);
     fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, xu);
-    GBS_LAUNCH_CHECK("time_pcg_apply setup");
-    const bool modal = ctx->modal_ok && modal_fits(nz);
     if (modal) {
-        const int r = modal_prepare<MODE_PCG>(ctx, nz);
+        fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.ap);
+        fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.s1);
+        fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.p0);
+        freeze_scalars_kernel<<<1, 1, 0, st>>>(w.sc);
+    }
+    GBS_LAUNCH_CHECK("time_pcg_apply setup");
+    if (modal) {
+        const int r = modal_prepare<MODE_CG>(ctx, nz);
         if (r < 0) return -r;
     }
     GraphCache *gc = (GraphCache *)ctx->graphs;
@@ -1129,7 +1201,7 @@ extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, co
     PcgArgs pa{w.r, w.dinv, w.p0, w.p1, xu, w.partials, w.sc};
     for (int i = 0; i < reps && rc == GBS_OK; ++i) {
         if (modal) {
-            rc = launch_modal<MODE_PCG>(ctx, nx, ny, nz, law, x, nullptr, w.ap, node_mask, pa, gc->cap);
+            rc = launch_modal<MODE_CG>(ctx, nx, ny, nz, law, x, nullptr, nullptr, node_mask, cg_args(w, xu), gc->cap);
         } else {
             TileArgs<float> A{nx, ny, nz, x, nullptr, w.ap, node_mask};
             const dim3 g = tile_grid<TileF>(nx, ny, nz), b = tile_block<TileF>();
@@ -1387,7 +1459,8 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
             const int64_t nd = n_dof_of(it.nx, it.ny, it.nz);
             SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
             PcgWs pw = pcg_ws(w.pcg, it.nx, it.ny, it.nz);
-            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, pw.p0, pw.p1, w.d32, pw.sc);
+            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, pw.p0, pw.p1, w.d32, pw.sc,
+                                                                    use_modal(ctx, it.nz) ? 0 : 1);
             GBS_LAUNCH_CHECK("pcg_finalize_kernel");
             GBS_CUDA_TRY(cudaMemcpyAsync((char *)hp + j * ps, pw.sc, ps, cudaMemcpyDeviceToHost, st));
         }
@@ -1397,7 +1470,7 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
             PcgScalars h;
             memcpy(&h, (char *)hp + j * ps, ps);
             if (std::find(pending.begin(), pending.end(), inn[k + j]) != pending.end())
-                count_launches(h.trips * (2 * kLoopUnroll + 1));
+                count_launches(h.trips * launches_per_trip(ctx, it.nz));
             it.stats.iterations += h.iter;
             if (h.status == GBS_EBREAKDOWN || h.status == GBS_ENONFINITE || h.status == GBS_ETIMEOUT) {
                 it.stats.status = h.status;
