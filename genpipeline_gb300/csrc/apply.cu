@@ -20,7 +20,8 @@ int launch_apply_plain(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<
 
 int apply_f32(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
               const float *p, float *y, const uint8_t *mask, cudaStream_t st) {
-    if (ctx->modal_ok && modal_fits(nz))
+    // the modal kernel copies p and writes y in aligned 16-byte groups
+    if (ctx->modal_ok && modal_fits(nz) && !((uintptr_t)p & 15) && !((uintptr_t)y & 15))
         return launch_modal<MODE_PLAIN>(ctx, nx, ny, nz, make_law<float>(*law), x, p, y, mask, CgArgs{}, st);
     return launch_apply_plain<TileF, float, KeF>(ctx, nx, ny, nz, make_law<float>(*law), ctx->kef, x, p, y, mask,
                                                  st);

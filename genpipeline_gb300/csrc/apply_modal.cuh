@@ -14,13 +14,16 @@
 // translation part of p_e cancels exactly in the first butterfly (FP32-friendly).
 //
 // Data movement: a CTA owns F consecutive nodes of the flattened (y,z) node plane
-// (flat = j*(nz+1) + k) and walks along x. Per step it computes one plane of the
-// F + nz + 2 elements touching those nodes (elements with k = nz are empty padding) from two
-// node planes held in shared memory (float4 per node, halo nz+2 on each side), while the
-// next node plane is loaded into registers. Contributions go to a per-corner shared array;
-// each owned node then sums the 4 (y,z) corners of element plane i (cx = 0) and keeps the
-// 4 of the x+1 side in registers for the next plane: one writer per node and DOF, fixed
-// summation order, no atomics.
+// (flat = j*(nz+1) + k) and walks along x. A plane's R = F + 2(nz+2) staged nodes are one
+// contiguous run of 3R words in every node vector, so each staged vector is copied as
+// 16-byte groups with cp.async (no registers held while the copies fly) into a raw buffer,
+// and combined group by group (float4) into the operand plane, laid out as one float4 per
+// node for the element gathers. Per step the CTA computes one plane of elements from two
+// operand planes while the copies of the plane after next are in flight. Each element's 24
+// corner contributions are combined along z with a warp shuffle (the element to the left
+// is the lane to the left), along y through a 6-float shared slot per element, and along x
+// in registers (the x+1 corners are carried to the next plane): one writer per node and DOF,
+// fixed summation order, no atomics. The owned nodes' results go out as float4 groups.
 #pragma once
 
 #include "apply_tile.cuh"
@@ -33,14 +36,30 @@ struct ModalGeom {
 };
 
 
-// Shared memory bytes of the modal kernel for a given z extent: three staged node planes
-// (six for the PCG modes, which also keep M r of each plane), two planes of element moduli
-// and the 24 corner contributions of every element of a plane.
+// Shared memory of the modal kernel for a given z extent (NT = 256, EPT = 2): three operand
+// planes of R + 2 float4 nodes, the raw cp.async buffers (one per staged vector: p for the
+// plain apply; r, w, s, 1/diag, p, x for the PCG modes) and the output words of a plane,
+// each 4 * ceil((3R + 3) / 4) floats, two planes of element moduli, the y-direction slots
+// (6 floats per element) and the warp-boundary contributions (12 floats per warp and lane).
 template <int NT, int EPT>
 inline size_t modal_smem_bytes(int nz, bool cg) {
     const int NE = NT * EPT, H = nz + 2, R = NE + H;
-    return (size_t)(cg ? 6 : 3) * R * sizeof(float4) + (size_t)2 * NE * sizeof(float) +
-           (size_t)24 * NE * sizeof(float);
+    const size_t RW = 4 * (size_t)((3 * R + 6) / 4);
+    return 3 * (size_t)(R + 2) * sizeof(float4) + ((cg ? 6 : 1) + 1) * RW * sizeof(float) +
+           (2 + 6) * (size_t)NT * sizeof(float2) + (size_t)(NT / 32) * 12 * sizeof(float2);
+}
+
+// cp.async (sm_80+): 16-byte global -> shared copies through L2 that use no registers;
+// src_bytes < 16 copies that many bytes and zero-fills the rest.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+__device__ __forceinline__ float2 shfl_up2(float2 v) {
+    return make_float2(__shfl_up_sync(0xffffffffu, v.x, 1), __shfl_up_sync(0xffffffffu, v.y, 1));
 }
 
 // Packed FP32x2 helpers (sm_100+): lane .x belongs to one element, lane .y to another.
@@ -135,16 +154,19 @@ __device__ __forceinline__ float ld_vec(const float *p) {
 
 // One sliding-window pass of a CTA over its (flat tile, x segment): y = D K D p on the owned
 // nodes (PLAIN), or one PCG iteration with y = w_{i+1} (CG modes). sums[] receives this
-// thread's FP32 shares of r.u, w.u and r.r (CG modes).
-template <int NT, int EPT, int MAXN, int MODE>
+// thread's FP32 shares of r.u, w.u and r.r (CG modes). Every node vector must be 16-byte
+// aligned.
+template <int NT, int EPT, int MAXV, int MODE>
 __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__restrict__ x,
                                            const float *__restrict__ p, float *__restrict__ y,
                                            const uint8_t *__restrict__ mask, const Law<float> &law,
-                                           const ModalK &km, const CgPass &cp, float4 *smem4, int tile, int seg,
+                                           const ModalK &km, const CgPass &cp, float *smem, int tile, int seg,
                                            float (&sums)[3]) {
     constexpr int NE = NT * EPT;
     constexpr bool CG = MODE == MODE_CG || MODE == MODE_CG_FUSED;
+    constexpr int NR = CG ? 6 : 1;  // staged vectors
     static_assert(EPT == 2, "two elements per thread (packed FP32x2)");
+    static_assert(NT % 32 == 0, "whole warps");
     static_assert(MODE == MODE_PLAIN || CG, "modal pass modes: PLAIN, CG, CG_FUSED");
 
     const int nx = G.nx, ny = G.ny, nz = G.nz;
@@ -152,86 +174,172 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
     const int S = (ny + 1) * NZ;  // nodes per x plane
     const int H = nz + 2;         // flat halo (one y row plus one node)
     const int R = NE + H;         // staged nodes per plane
-    const int F = NE - H;         // owned nodes per plane
+    const int F = NE - H;         // owned nodes per plane (chunk positions [H, NE))
     const int F0 = tile * F;
     const int xs = seg * G.seglen;
     const int xe = min(xs + G.seglen, nx + 1);
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int RW = 4 * ((3 * R + 6) / 4);
+    const int64_t NW = 3LL * (nx + 1) * S;  // words of a node vector
 
-    float4 *Pn = smem4;                               // [3][R] operand planes (x, y, z, unused)
-    float4 *Zn = Pn + 3 * R;                          // [3][R] M r_i of the same planes (CG)
-    float2 *Es2 = (float2 *)(Pn + (CG ? 6 : 3) * R);  // [2][NT] element moduli (tid, tid + NT)
-    float2 *Cc2 = Es2 + 2 * NT;                       // [24][NT] corner contributions (tid, tid + NT)
-    const float *Cc = (const float *)Cc2;
+    float4 *Pn = (float4 *)smem;                // [3][R + 2] operand planes; chunk node l at 1 + l
+    float *Raw = (float *)(Pn + 3 * (R + 2));   // [NR][RW] cp.async buffers
+    float *Ys = Raw + NR * RW;                  // [RW] output words of the plane
+    float2 *Es2 = (float2 *)(Ys + RW);          // [2][NT] element moduli (tid, tid + NT)
+    float2 *Z1s = Es2 + 2 * NT;                 // [6][NT] y+1-side contributions (cx, c) per element
+    float2 *Bd = Z1s + 6 * NT;                  // [NT/32][12] z+1-side contributions of lane 31
+    const float *Z1f = (const float *)Z1s;
+    const float *Bdf = (const float *)Bd;
 
     const float alpha = cp.alpha, beta = cp.beta;
     float g_ru = 0.0f, g_wu = 0.0f, g_rr = 0.0f;  // FP32 per-thread partials
 
-    // ---- staging: issue the loads of a plane now, combine and store them later, so that
-    // the element work of the current plane hides their latency ------------------------
-    float ra[MAXN][3], rb[MAXN][3], rc[MAXN][3], rd[MAXN][3];  // PLAIN: p; CG: r_i, w_i, s_{i-1}, M
-    uint8_t rm[MAXN];
-    float ex[EPT];
-    bool eok[EPT];
-    auto stage_node = [&](int l, int j, int64_t &n) -> bool {
-        const int flat = F0 - H + l;
-        const bool ok = l < R && j >= 0 && j <= nx && flat >= 0 && flat < S;
-        n = ok ? (int64_t)j * S + flat : 0;
-        return ok;
+    auto src_of = [&](int a) -> const float * {
+        if (!CG) return p;
+        return a == 0 ? cp.r : a == 1 ? cp.w : a == 2 ? cp.sold : a == 3 ? cp.dinv : a == 4 ? cp.p : cp.xu;
     };
+    // Word geometry of node plane j: the chunk's words start at W0 = 3 (j S + F0 - H); group f
+    // holds the aligned words [A + 4f, A + 4f + 4), chunk words 4f - pad .. 4f - pad + 3.
+    struct PlaneW {
+        int64_t A;
+        int pad, nv, lo3, hi3, olo3, ohi3;
+        bool pv, own;
+    };
+    auto plane_w = [&](int j) {
+        PlaneW P;
+        const int64_t W0 = 3 * ((int64_t)j * S + F0 - H);
+        P.A = W0 & ~(int64_t)3;
+        P.pad = (int)(W0 - P.A);
+        P.nv = (P.pad + 3 * R + 3) / 4;
+        P.pv = j >= 0 && j <= nx;
+        P.lo3 = 3 * max(0, H - F0);          // chunk words of nodes inside the plane
+        P.hi3 = 3 * min(R, S - F0 + H);
+        P.own = j >= xs && j < xe;
+        P.olo3 = 3 * H;                      // chunk words of owned nodes
+        P.ohi3 = 3 * min(NE, S - F0 + H);
+        return P;
+    };
+
+    // ---- staging ---------------------------------------------------------------------------
     auto issue_plane = [&](int j) {
+        const PlaneW P = plane_w(j);
 #pragma unroll
-        for (int q = 0; q < MAXN; ++q) {
-            int64_t n;
-            const bool ok = stage_node(tid + q * NT, j, n);
+        for (int q = 0; q < MAXV; ++q) {
+            const int f = tid + q * NT;
+            if (f < P.nv) {
+                const int cw0 = 4 * f - P.pad;
+                const int64_t gw = P.A + 4 * (int64_t)f;
+                int nb = 0;  // bytes of the group inside the vector, when it meets the plane's nodes
+                if (P.pv && cw0 + 4 > P.lo3 && cw0 < P.hi3 && gw >= 0 && gw < NW)
+                    nb = 4 * (int)(NW - gw < 4 ? NW - gw : 4);
+                const bool ownable = P.own && cw0 + 4 > P.olo3 && cw0 < P.ohi3;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                if (!CG) {
-                    ra[q][c] = ok ? p[3 * n + c] : 0.0f;
-                } else {
-                    ra[q][c] = ok ? ld_vec<MODE>(&cp.r[3 * n + c]) : 0.0f;
-                    rb[q][c] = ok ? ld_vec<MODE>(&cp.w[3 * n + c]) : 0.0f;
-                    rc[q][c] = ok ? ld_vec<MODE>(&cp.sold[3 * n + c]) : 0.0f;
-                    rd[q][c] = ok ? cp.dinv[3 * n + c] : 0.0f;
+                for (int a = 0; a < NR; ++a) {
+                    const bool need = a < 4 || ownable;  // p and x only where nodes are owned
+                    if (nb > 0 && need) cp_async16(Raw + a * RW + 4 * f, src_of(a) + gw, nb);
                 }
             }
-            if (!CG) rm[q] = (ok && mask) ? mask[n] : (uint8_t)0;
         }
+        cp_async_commit();
     };
+    // Combines the staged groups of plane j (this thread's own copies) into operand slot
+    // `slot`; in the PCG modes also updates s, r, p and x of the owned words.
     auto commit_plane = [&](int slot, int j) {
+        const PlaneW P = plane_w(j);
+        cp_async_wait_all();
+        float *Pf = (float *)(Pn + slot * (R + 2) + 1);  // word 4 l + c of chunk node l
 #pragma unroll
-        for (int q = 0; q < MAXN; ++q) {
-            const int l = tid + q * NT;
-            if (!CG) {
-                float v[3];
+        for (int q = 0; q < MAXV; ++q) {
+            const int f = tid + q * NT;
+            if (f < P.nv) {
+                const int cw0 = 4 * f - P.pad;
+                const int64_t gw = P.A + 4 * (int64_t)f;
+                bool valid[4], own[4];
+                bool all_own = true;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) v[c] = ((rm[q] >> c) & 1) ? 0.0f : ra[q][c];
-                if (l < R) Pn[slot * R + l] = make_float4(v[0], v[1], v[2], 0.0f);
-            } else {
-                int64_t n;
-                const bool ok = stage_node(l, j, n);
-                const bool own = ok && l >= H && l < NE && j >= xs && j < xe;
-                float u[3], z[3];
+                for (int k = 0; k < 4; ++k) {
+                    const int cw = cw0 + k;
+                    valid[k] = P.pv && cw >= P.lo3 && cw < P.hi3;
+                    own[k] = valid[k] && P.own && cw >= P.olo3 && cw < P.ohi3;
+                    all_own = all_own && own[k];
+                }
+                float val[4];
+                if (!CG) {
+                    const float4 a4 = *(const float4 *)(Raw + 4 * f);
+                    const float av[4] = {a4.x, a4.y, a4.z, a4.w};
 #pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const float s = fmaf(beta, rc[q][c], rb[q][c]);
-                    const float rn = fmaf(-alpha, s, ra[q][c]);
-                    u[c] = rd[q][c] * rn;
-                    z[c] = rd[q][c] * ra[q][c];
-                    if (own) {
-                        cp.snew[3 * n + c] = s;
-                        cp.rnew[3 * n + c] = rn;
-                        g_ru = fmaf(rn, u[c], g_ru);
-                        g_rr = fmaf(rn, rn, g_rr);
+                    for (int k = 0; k < 4; ++k) {
+                        bool fixed = false;
+                        if (mask && valid[k]) {
+                            const int cw = cw0 + k, l = cw / 3;
+                            fixed = (mask[(int64_t)j * S + F0 - H + l] >> (cw - 3 * l)) & 1;
+                        }
+                        val[k] = valid[k] && !fixed ? av[k] : 0.0f;
+                    }
+                } else {
+                    const float4 r4 = *(const float4 *)(Raw + 0 * RW + 4 * f);
+                    const float4 w4 = *(const float4 *)(Raw + 1 * RW + 4 * f);
+                    const float4 s4 = *(const float4 *)(Raw + 2 * RW + 4 * f);
+                    const float4 d4 = *(const float4 *)(Raw + 3 * RW + 4 * f);
+                    const float rv[4] = {r4.x, r4.y, r4.z, r4.w}, wv[4] = {w4.x, w4.y, w4.z, w4.w};
+                    const float sv[4] = {s4.x, s4.y, s4.z, s4.w}, dv[4] = {d4.x, d4.y, d4.z, d4.w};
+                    float so[4], rno[4], po[4], xo[4];
+                    const bool any_own = own[0] || own[1] || own[2] || own[3];
+                    float pv4[4] = {0.0f, 0.0f, 0.0f, 0.0f}, xv4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                    if (any_own) {
+                        const float4 p4 = *(const float4 *)(Raw + 4 * RW + 4 * f);
+                        const float4 x4 = *(const float4 *)(Raw + 5 * RW + 4 * f);
+                        pv4[0] = p4.x, pv4[1] = p4.y, pv4[2] = p4.z, pv4[3] = p4.w;
+                        xv4[0] = x4.x, xv4[1] = x4.y, xv4[2] = x4.z, xv4[3] = x4.w;
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const float s = fmaf(beta, sv[k], wv[k]);
+                        const float rn = fmaf(-alpha, s, rv[k]);
+                        const float u = dv[k] * rn;
+                        val[k] = valid[k] ? u : 0.0f;
+                        so[k] = s;
+                        rno[k] = rn;
+                        po[k] = fmaf(beta, pv4[k], dv[k] * rv[k]);
+                        xo[k] = fmaf(alpha, po[k], xv4[k]);
+                        if (own[k]) {
+                            g_ru = fmaf(rn, u, g_ru);
+                            g_rr = fmaf(rn, rn, g_rr);
+                        }
+                    }
+                    if (all_own) {
+                        *(float4 *)(cp.snew + gw) = make_float4(so[0], so[1], so[2], so[3]);
+                        *(float4 *)(cp.rnew + gw) = make_float4(rno[0], rno[1], rno[2], rno[3]);
+                        *(float4 *)(cp.p + gw) = make_float4(po[0], po[1], po[2], po[3]);
+                        *(float4 *)(cp.xu + gw) = make_float4(xo[0], xo[1], xo[2], xo[3]);
+                    } else if (any_own) {
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (own[k]) {
+                                cp.snew[gw + k] = so[k];
+                                cp.rnew[gw + k] = rno[k];
+                                cp.p[gw + k] = po[k];
+                                cp.xu[gw + k] = xo[k];
+                            }
                     }
                 }
-                if (l < R) {
-                    Pn[slot * R + l] = make_float4(u[0], u[1], u[2], 0.0f);
-                    Zn[slot * R + l] = make_float4(z[0], z[1], z[2], 0.0f);
+                // scatter into the node layout: chunk word cw = 3 l + c -> Pf[4 l + c]
+                // (cw0 >= -3, so l >= -1; l <= R; both ends are spare slots)
+                int l = (cw0 + 3) / 3 - 1;
+                int c = cw0 - 3 * l;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    Pf[4 * l + c] = val[k];
+                    if (++c == 3) {
+                        c = 0;
+                        ++l;
+                    }
                 }
             }
         }
     };
+    float ex[EPT];
+    bool eok[EPT];
     auto issue_eplane = [&](int j) {
 #pragma unroll
         for (int q = 0; q < EPT; ++q) {
@@ -244,6 +352,12 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
     auto commit_eplane = [&](int slot) {
         Es2[slot * NT + tid] =
             make_float2(eok[0] ? modulus(law, ex[0]) : 0.0f, eok[1] ? modulus(law, ex[1]) : 0.0f);
+    };
+    // z+1-side contribution (cx, cy, c) of element e - 1 where e sits in lane 0
+    auto boundary = [&](int e, int cx, int cy, int c) -> float {
+        const int pe = e - 1;
+        const int pt = pe >= NT ? pe - NT : pe;
+        return Bdf[2 * ((pt >> 5) * 12 + (cx * 2 + cy) * 3 + c) + (pe >= NT ? 1 : 0)];
     };
 
     // ---- prologue: node planes xs-1, xs and element plane xs-1 --------------------------
@@ -267,100 +381,115 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
         const bool more_elems = i + 1 <= xe - 1;
         if (more_nodes) issue_plane(i + 2);
         if (more_elems) issue_eplane(i + 1);
-        // owned-node operands of plane i, loaded before the element work as well
         const bool out_plane = i >= xs;
         uint8_t om[EPT];
-        float ox[EPT][3], op[EPT][3];
 #pragma unroll
         for (int q = 0; q < EPT; ++q) {
-            const int t = tid + q * NT;
-            const bool ok = out_plane && t < F && F0 + t < S;
-            const int64_t n = ok ? (int64_t)i * S + F0 + t : 0;
-            om[q] = (ok && mask) ? mask[n] : (uint8_t)0;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                if (CG) {
-                    ox[q][c] = ok ? ld_vec<MODE>(&cp.xu[3 * n + c]) : 0.0f;
-                    op[q][c] = ok ? ld_vec<MODE>(&cp.p[3 * n + c]) : 0.0f;
-                } else {
-                    ox[q][c] = op[q][c] = 0.0f;
-                }
-            }
+            const int l = tid + q * NT;
+            const bool ok = out_plane && l >= H && F0 - H + l < S;
+            om[q] = (ok && mask) ? mask[(int64_t)i * S + F0 - H + l] : (uint8_t)0;
         }
 
         // ---- element plane i: elements tid and tid + NT as the two lanes of a float2 ----
+        float2 v[8][3];
         if (i >= 0 && i < nx) {
             const float2 E = Es2[es * NT + tid];
-            float2 v[8][3];
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
                 const int cx = b >> 2, cy = (b >> 1) & 1, cz = b & 1;
-                const float4 *src = Pn + (cx ? s1 : s0) * R + tid + cy * NZ + cz;
+                const float4 *src = Pn + (cx ? s1 : s0) * (R + 2) + 1 + tid + cy * NZ + cz;
                 const float4 wa = src[0], wb = src[NT];
                 v[b][0] = make_float2(wa.x, wb.x);
                 v[b][1] = make_float2(wa.y, wb.y);
                 v[b][2] = make_float2(wa.z, wb.z);
             }
             modal_element2(v, E, km);
+        } else {
 #pragma unroll
             for (int b = 0; b < 8; ++b)
 #pragma unroll
-                for (int c = 0; c < 3; ++c) Cc2[(b * 3 + c) * NT + tid] = v[b][c];
-        } else {
+                for (int c = 0; c < 3; ++c) v[b][c] = make_float2(0.0f, 0.0f);
+        }
+        // z: the cz = 1 corners of element e - 1 (lane - 1) join the cz = 0 corners of e
+        float2 z0[2][3];
 #pragma unroll
-            for (int kk = 0; kk < 24; ++kk) Cc2[kk * NT + tid] = make_float2(0.0f, 0.0f);
+        for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float2 a1 = shfl_up2(v[cx * 4 + 1][c]), b1 = shfl_up2(v[cx * 4 + 3][c]);
+                if (lane == 0) a1 = b1 = make_float2(0.0f, 0.0f);
+                z0[cx][c] = add2(v[cx * 4 + 0][c], a1);
+                Z1s[(cx * 3 + c) * NT + tid] = add2(v[cx * 4 + 2][c], b1);
+            }
+        if (lane == 31) {
+#pragma unroll
+            for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+                for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) Bd[warp * 12 + (cx * 2 + cy) * 3 + c] = v[cx * 4 + cy * 2 + 1][c];
         }
         if (more_nodes) commit_plane(s2, i + 2);
         if (more_elems) commit_eplane(es ^ 1);
         __syncthreads();
 
-        // ---- owned nodes of plane i ------------------------------------------------------
+        // ---- nodes of plane i: node l = element l of this thread --------------------------
+        const float4 *Pu = Pn + s0 * (R + 2) + 1;
+        const PlaneW Pi = plane_w(i);
 #pragma unroll
         for (int q = 0; q < EPT; ++q) {
-            const int t = tid + q * NT;
-            if (t < F) {
-                const int te[4] = {t + H, t + H - 1, t + 1, t};  // (cy,cz) = 00, 01, 10, 11
-                int ce[4];  // float offset of element te in a Cc2 row
+            const int l = tid + q * NT;
+            if (l >= H) {
+                const int m = l - NZ;  // element whose y+1 corners touch node l (m >= 1)
+                const int mi = m >= NT ? 2 * (m - NT) + 1 : 2 * m;
+                float yy[2][3];
 #pragma unroll
-                for (int yz = 0; yz < 4; ++yz) ce[yz] = te[yz] >= NT ? 2 * (te[yz] - NT) + 1 : 2 * te[yz];
-                float yv[3], nacc[3];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    float s = acc[q][c], a1 = 0.0f;
-#pragma unroll
-                    for (int yz = 0; yz < 4; ++yz) {
-                        s += Cc[(yz * 3 + c) * 2 * NT + ce[yz]];
-                        a1 += Cc[((4 + yz) * 3 + c) * 2 * NT + ce[yz]];
-                    }
-                    yv[c] = s;
-                    nacc[c] = a1;
-                }
-                const int flat = F0 + t;
-                if (out_plane && flat < S) {
-                    const int64_t n = (int64_t)i * S + flat;
-                    float uc[3] = {0.0f, 0.0f, 0.0f}, zc[3] = {0.0f, 0.0f, 0.0f};
-                    if (CG) {
-                        const float4 wu = Pn[s0 * R + t + H], wz = Zn[s0 * R + t + H];
-                        uc[0] = wu.x, uc[1] = wu.y, uc[2] = wu.z;
-                        zc[0] = wz.x, zc[1] = wz.y, zc[2] = wz.z;
-                    }
+                for (int cx = 0; cx < 2; ++cx)
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        const float yc = ((om[q] >> c) & 1) ? 0.0f : yv[c];
-                        y[3 * n + c] = yc;
-                        if (CG) {
-                            g_wu = fmaf(uc[c], yc, g_wu);
-                            const float pc = fmaf(beta, op[q][c], zc[c]);
-                            cp.p[3 * n + c] = pc;
-                            cp.xu[3 * n + c] = fmaf(alpha, pc, ox[q][c]);
-                        }
+                        float s = (q ? z0[cx][c].y : z0[cx][c].x) + Z1f[(cx * 3 + c) * 2 * NT + mi];
+                        if (lane == 0) s += boundary(l, cx, 0, c);
+                        if ((m & 31) == 0) s += boundary(m, cx, 1, c);
+                        yy[cx][c] = s;
+                    }
+                const int flat = F0 - H + l;
+                if (out_plane && flat < S) {
+                    const float4 u4 = Pu[l];
+                    const float uc[3] = {u4.x, u4.y, u4.z};
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float yc = ((om[q] >> c) & 1) ? 0.0f : acc[q][c] + yy[0][c];
+                        if (CG) g_wu = fmaf(uc[c], yc, g_wu);
+                        Ys[Pi.pad + 3 * l + c] = yc;
                     }
                 }
 #pragma unroll
-                for (int c = 0; c < 3; ++c) acc[q][c] = nacc[c];
+                for (int c = 0; c < 3; ++c) acc[q][c] = yy[1][c];
             }
         }
         __syncthreads();
+
+        // ---- owned words of plane i out as float4 groups -----------------------------------
+        if (out_plane) {
+            const PlaneW &P = Pi;
+#pragma unroll
+            for (int q = 0; q < MAXV; ++q) {
+                const int f = tid + q * NT;
+                const int cw0 = 4 * f - P.pad;
+                if (f < P.nv && cw0 + 4 > P.olo3 && cw0 < P.ohi3) {
+                    const int64_t gw = P.A + 4 * (int64_t)f;
+                    const float4 y4 = *(const float4 *)(Ys + 4 * f);
+                    if (cw0 >= P.olo3 && cw0 + 4 <= P.ohi3) {
+                        *(float4 *)(y + gw) = y4;
+                    } else {
+                        const float yv[4] = {y4.x, y4.y, y4.z, y4.w};
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if (cw0 + k >= P.olo3 && cw0 + k < P.ohi3) y[gw + k] = yv[k];
+                    }
+                }
+            }
+        }
     }
     sums[0] = g_ru;
     sums[1] = g_wu;
@@ -400,7 +529,7 @@ __device__ __forceinline__ void cg_scalar_step(double gamma, double delta, doubl
     }
 }
 
-template <int NT, int EPT, int MAXN, int MODE>
+template <int NT, int EPT, int MAXV, int MODE>
 __global__ void __launch_bounds__(NT, 2)
     apply_modal_kernel(ModalGeom G, const float *__restrict__ x, const float *__restrict__ p, float *__restrict__ y,
                        const uint8_t *__restrict__ mask, Law<float> law, const ModalK km, CgArgs ca) {
@@ -415,12 +544,16 @@ __global__ void __launch_bounds__(NT, 2)
         it = sc->iter;
         const double a = sc->alpha[0], b = sc->beta;
         if (done) return;
-        const int c = it & 1, nc = c ^ 1;
-        cp = CgPass{(float)a, (float)b, ca.r[c], ca.w[c], ca.s[nc], ca.dinv, ca.r[nc], ca.s[c], ca.p, ca.xu};
-        y = ca.w[nc];
+        // parity selects (a dynamic index into the parameter arrays would copy them to the stack)
+        const bool odd = it & 1;
+        float *r_c = odd ? ca.r[1] : ca.r[0], *r_n = odd ? ca.r[0] : ca.r[1];
+        float *w_c = odd ? ca.w[1] : ca.w[0], *w_n = odd ? ca.w[0] : ca.w[1];
+        float *s_c = odd ? ca.s[1] : ca.s[0], *s_n = odd ? ca.s[0] : ca.s[1];
+        cp = CgPass{(float)a, (float)b, r_c, w_c, s_n, ca.dinv, r_n, s_c, ca.p, ca.xu};
+        y = w_n;
     }
     float sums[3];
-    modal_pass<NT, EPT, MAXN, MODE>(G, x, p, y, mask, law, km, cp, smem4, blockIdx.x, blockIdx.y, sums);
+    modal_pass<NT, EPT, MAXV, MODE>(G, x, p, y, mask, law, km, cp, (float *)smem4, blockIdx.x, blockIdx.y, sums);
     if (MODE == MODE_CG) {
         const int nblk = gridDim.x * gridDim.y;
         const int bid = blockIdx.x + gridDim.x * blockIdx.y;
@@ -494,8 +627,9 @@ inline dim3 modal_grid(const ModalGeom &g) {
     return dim3((unsigned)((S + F - 1) / F), (unsigned)g.nseg, 1);
 }
 
-// Staged nodes per thread: R / NT = EPT + ceil((nz + 2) / NT).
-inline bool modal_small_halo(int nz) { return nz + 2 <= kModalNT; }
+// 16-byte groups of a staged plane per thread: 2 when 4 * ceil((3R + 3) / 4) <= 8 NT words
+// (nz <= 166), else 3 (modal_fits bounds nz).
+inline bool modal_short(int nz) { return (3 * (kModalNT * kModalEPT + nz + 2) + 6) / 4 <= 2 * kModalNT; }
 
 // Resident CTAs per SM of a kernel that uses `smem` bytes of dynamic shared memory: the
 // register limit (occupancy at no dynamic shared memory, queried once per device) and the
@@ -516,9 +650,9 @@ inline int modal_resident(const gbsimp_ctx *ctx, const void *kern, int &reg_cach
 
 // Sets the kernel's dynamic shared-memory limit once per device (host calls only; done before
 // any graph capture) and returns resident CTAs per SM for this z extent, or < 0 on error.
-template <int MODE, int MAXN>
+template <int MODE, int MAXV>
 inline int modal_prepare_one(const gbsimp_ctx *ctx, int nz) {
-    auto kern = apply_modal_kernel<kModalNT, kModalEPT, MAXN, MODE>;
+    auto kern = apply_modal_kernel<kModalNT, kModalEPT, MAXV, MODE>;
     constexpr bool cg = MODE != MODE_PLAIN;
     static int set_cache[128] = {};  // benign races: every thread stores the same values
     static int reg_cache[128] = {};
@@ -534,8 +668,7 @@ inline int modal_prepare_one(const gbsimp_ctx *ctx, int nz) {
 
 template <int MODE>
 inline int modal_prepare(const gbsimp_ctx *ctx, int nz) {
-    return modal_small_halo(nz) ? modal_prepare_one<MODE, kModalEPT + 1>(ctx, nz)
-                                : modal_prepare_one<MODE, kModalEPT + 2>(ctx, nz);
+    return modal_short(nz) ? modal_prepare_one<MODE, 2>(ctx, nz) : modal_prepare_one<MODE, 3>(ctx, nz);
 }
 
 // Launches the modal kernel (MODE_PLAIN: y = D K D p; MODE_CG: one PCG iteration).
@@ -546,11 +679,11 @@ inline int launch_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law
     if (per_sm < 0) return -per_sm;
     const size_t smem = modal_smem_bytes<kModalNT, kModalEPT>(nz, MODE != MODE_PLAIN);
     const ModalGeom g = modal_geom(nx, ny, nz, ctx->num_sms, per_sm);
-    if (modal_small_halo(nz))
-        apply_modal_kernel<kModalNT, kModalEPT, kModalEPT + 1, MODE>
+    if (modal_short(nz))
+        apply_modal_kernel<kModalNT, kModalEPT, 2, MODE>
             <<<modal_grid(g), kModalNT, smem, st>>>(g, x, p, y, mask, law, ctx->km, ca);
     else
-        apply_modal_kernel<kModalNT, kModalEPT, kModalEPT + 2, MODE>
+        apply_modal_kernel<kModalNT, kModalEPT, 3, MODE>
             <<<modal_grid(g), kModalNT, smem, st>>>(g, x, p, y, mask, law, ctx->km, ca);
     GBS_LAUNCH_CHECK("apply_modal_kernel");
     return GBS_OK;

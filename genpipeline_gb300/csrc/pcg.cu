@@ -60,12 +60,17 @@ static size_t pcg_partials(int nx, int ny, int nz) {
 
 static size_t pcg_ws_bytes_impl(int nx, int ny, int nz) {
     const size_t nd = (size_t)n_dof_of(nx, ny, nz);
-    return al256(sizeof(PcgScalars)) + 8 * al256(nd * sizeof(float)) + al256(pcg_partials(nx, ny, nz) * sizeof(double));
+    return 256 + al256(sizeof(PcgScalars)) + 8 * al256(nd * sizeof(float)) +
+           al256(pcg_partials(nx, ny, nz) * sizeof(double));
 }
+
+// Sub-buffers start on 256-byte boundaries whatever the alignment of `ws` (the size has
+// 256 bytes of slack); the modal kernels copy vectors in aligned 16-byte groups.
+static char *align256(void *ws) { return (char *)(((uintptr_t)ws + 255) & ~(uintptr_t)255); }
 
 static PcgWs pcg_ws(void *ws, int nx, int ny, int nz) {
     const size_t nd = (size_t)n_dof_of(nx, ny, nz);
-    char *p = (char *)ws;
+    char *p = align256(ws);
     PcgWs w;
     w.sc = (PcgScalars *)p;
     p += al256(sizeof(PcgScalars));
@@ -412,7 +417,7 @@ struct FusedTable {
     FusedDesign d[kMaxFused];
 };
 
-template <int NT, int EPT, int MAXN>
+template <int NT, int EPT, int MAXV>
 __global__ void __launch_bounds__(NT, 2)
     pcg_fused_kernel(const __grid_constant__ FusedTable T, Law<float> law, const ModalK km,
                      unsigned long long wait_ns) {
@@ -438,7 +443,7 @@ __global__ void __launch_bounds__(NT, 2)
         const int c = it & 1, nc = c ^ 1;
         const CgPass cp{(float)alpha, (float)beta, ca.r[c], ca.w[c], ca.s[nc], ca.dinv, ca.r[nc], ca.s[c], ca.p, ca.xu};
         float sums[3];
-        modal_pass<NT, EPT, MAXN, MODE_CG_FUSED>(G, D.x, nullptr, ca.w[nc], D.mask, law, km, cp, smem4, tile, seg,
+        modal_pass<NT, EPT, MAXV, MODE_CG_FUSED>(G, D.x, nullptr, ca.w[nc], D.mask, law, km, cp, (float *)smem4, tile, seg,
                                                  sums);
         __threadfence();
         target += nblk;
@@ -491,11 +496,11 @@ static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n,
     int max_nz = 0;
     for (int i = 0; i < n; ++i) {
         if (!modal_fits(items[i].nz)) return GBS_EINVAL;
-        small = small && modal_small_halo(items[i].nz);
+        small = small && modal_short(items[i].nz);
         max_nz = items[i].nz > max_nz ? items[i].nz : max_nz;
     }
-    void *kern = small ? (void *)pcg_fused_kernel<kModalNT, kModalEPT, kModalEPT + 1>
-                       : (void *)pcg_fused_kernel<kModalNT, kModalEPT, kModalEPT + 2>;
+    void *kern = small ? (void *)pcg_fused_kernel<kModalNT, kModalEPT, 2>
+                       : (void *)pcg_fused_kernel<kModalNT, kModalEPT, 3>;
     static int ready_cache[2][128] = {};  // 1 = attribute set and cooperative launch supported, -1 = not
     static int reg_cache[2][128] = {};
     const int dev = ctx->device >= 0 && ctx->device < 128 ? ctx->device : 0;
@@ -855,13 +860,13 @@ struct SolveWs {
 
 static size_t solve_ws_bytes_impl(int nx, int ny, int nz) {
     const size_t nd = (size_t)n_dof_of(nx, ny, nz);
-    return al256(sizeof(OuterScalars)) + al256(nd * 8) + 2 * al256(nd * 4) + al256(3 * 4096 * 8) +
-           pcg_ws_bytes_impl(nx, ny, nz) + al256(apply_f64_modal_ws_bytes(nx, ny, nz));
+    return 256 + al256(sizeof(OuterScalars)) + al256(nd * 8) + 2 * al256(nd * 4) + al256(3 * 4096 * 8) +
+           al256(pcg_ws_bytes_impl(nx, ny, nz)) + al256(apply_f64_modal_ws_bytes(nx, ny, nz));
 }
 
 static SolveWs solve_ws(void *ws, int nx, int ny, int nz) {
     const size_t nd = (size_t)n_dof_of(nx, ny, nz);
-    char *p = (char *)ws;
+    char *p = align256(ws);
     SolveWs w;
     w.os = (OuterScalars *)p;
     p += al256(sizeof(OuterScalars));
@@ -1170,7 +1175,7 @@ extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, co
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t nd = n_dof_of(nx, ny, nz);
     PcgWs w = pcg_ws(ws, nx, ny, nz);
-    float *xu = (float *)((char *)ws + pcg_ws_bytes_impl(nx, ny, nz));
+    float *xu = (float *)(align256(ws) + pcg_ws_bytes_impl(nx, ny, nz) - 256);
     const Law<float> law = make_law<float>(*glaw);
     // A state on which every launch does the full work of one iteration and repeats it:
     // r = 1, everything else 0 (alpha = beta = 0), iteration 0. Single-reduction kernel: the
@@ -1256,6 +1261,7 @@ extern "C" int gbsimp_pcg_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbs
     if (!ctx || !law || !x || !b || !u || !opts || !ws || !grid_ok(nx, ny, nz))
         return set_error(GBS_EINVAL, "gbsimp_pcg_f32: bad arguments");
     if (ws_bytes < pcg_ws_bytes_impl(nx, ny, nz)) return set_error(GBS_EINVAL, "gbsimp_pcg_f32: workspace too small");
+    if ((uintptr_t)u & 15) return set_error(GBS_EINVAL, "gbsimp_pcg_f32: u must be 16-byte aligned");
     PcgScalars h;
     ApplyProfile prof;
     int rc = pcg_run(ctx, nx, ny, nz, law, x, b, node_mask, u, opts->rtol, opts->max_iter, opts->check_every, ws, &h,
