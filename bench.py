@@ -356,12 +356,19 @@ def run_ours(a):
     e2e = {"value": world * a.steps / te, "unit": UNIT, "h2d_bytes_per_step": 4 * ne,
            "d2h_bytes_per_step": 8 * ne}
 
-    # ---- roofline of the dominant kernel (the fused PCG apply, K1) ----------------------
-    alg_bytes = 4 * (7 * nd + ne)  # r, dinv, p_old, x_u, x in; p_new, Ap, x_u out
+    # ---- roofline of the dominant kernel (the one-kernel PCG iteration) -----------------
+    path = prob.eng.apply_path(GRID[2])
+    if path == "modal":
+        # r_i, w_i, s_{i-1}, 1/diag, p_{i-1}, x_i and the densities in; s_i, r_{i+1}, p_i,
+        # x_{i+1}, w_{i+1} out
+        alg_bytes = 4 * (11 * nd + ne)
+        kname = "apply_modal_kernel<CG> (one single-reduction PCG iteration: s, r, u staging, w = DKDu, p, x)"
+    else:
+        alg_bytes = 4 * (7 * nd + ne)  # r, dinv, p_old, x_u, x in; p_new, Ap, x_u out
+        kname = "apply_tile_kernel<PCG> (K(x)p fused with p = z + beta p, x update, p.Ap)"
     peak, peak_src = _measured_peak()
     achieved = alg_bytes / per_launch / 1e9
-    path = prob.eng.apply_path(GRID[2])
-    roof = {"bound": "hbm", "kernel": f"apply_{path}_kernel<PCG> (K(x)p fused with p = z + beta p, x update, p.Ap)",
+    roof = {"bound": "hbm", "kernel": kname,
             "achieved": achieved, "peak": peak, "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak,
             "traffic": _profiled_traffic(a.workload), "alg_bytes_per_launch": alg_bytes, "launch_us": per_launch * 1e6,
             "fp32_flops_per_launch_dense_equiv": 1152 * ne,

@@ -243,7 +243,8 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
         cp_async_commit();
     };
     // Combines the staged groups of plane j (this thread's own copies) into operand slot
-    // `slot`; in the PCG modes also updates s, r, p and x of the owned words.
+    // `slot`; in the PCG modes also updates s, r, p and x of the owned words. Interior groups
+    // (all four words inside the plane, and all or none owned) take a branch-free path.
     auto commit_plane = [&](int slot, int j) {
         const PlaneW P = plane_w(j);
         cp_async_wait_all();
@@ -254,27 +255,23 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
             if (f < P.nv) {
                 const int cw0 = 4 * f - P.pad;
                 const int64_t gw = P.A + 4 * (int64_t)f;
-                bool valid[4], own[4];
-                bool all_own = true;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const int cw = cw0 + k;
-                    valid[k] = P.pv && cw >= P.lo3 && cw < P.hi3;
-                    own[k] = valid[k] && P.own && cw >= P.olo3 && cw < P.ohi3;
-                    all_own = all_own && own[k];
-                }
+                const bool in_all = P.pv && cw0 >= P.lo3 && cw0 + 4 <= P.hi3;
+                const bool own_all = in_all && P.own && cw0 >= P.olo3 && cw0 + 4 <= P.ohi3;
+                const bool own_none = !P.own || cw0 + 4 <= P.olo3 || cw0 >= P.ohi3;
                 float val[4];
                 if (!CG) {
                     const float4 a4 = *(const float4 *)(Raw + 4 * f);
                     const float av[4] = {a4.x, a4.y, a4.z, a4.w};
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
+                        const int cw = cw0 + k;
+                        const bool valid = in_all || (P.pv && cw >= P.lo3 && cw < P.hi3);
                         bool fixed = false;
-                        if (mask && valid[k]) {
-                            const int cw = cw0 + k, l = cw / 3;
+                        if (mask && valid) {
+                            const int l = cw / 3;
                             fixed = (mask[(int64_t)j * S + F0 - H + l] >> (cw - 3 * l)) & 1;
                         }
-                        val[k] = valid[k] && !fixed ? av[k] : 0.0f;
+                        val[k] = valid && !fixed ? av[k] : 0.0f;
                     }
                 } else {
                     const float4 r4 = *(const float4 *)(Raw + 0 * RW + 4 * f);
@@ -283,58 +280,67 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
                     const float4 d4 = *(const float4 *)(Raw + 3 * RW + 4 * f);
                     const float rv[4] = {r4.x, r4.y, r4.z, r4.w}, wv[4] = {w4.x, w4.y, w4.z, w4.w};
                     const float sv[4] = {s4.x, s4.y, s4.z, s4.w}, dv[4] = {d4.x, d4.y, d4.z, d4.w};
-                    float so[4], rno[4], po[4], xo[4];
-                    const bool any_own = own[0] || own[1] || own[2] || own[3];
-                    float pv4[4] = {0.0f, 0.0f, 0.0f, 0.0f}, xv4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-                    if (any_own) {
-                        const float4 p4 = *(const float4 *)(Raw + 4 * RW + 4 * f);
-                        const float4 x4 = *(const float4 *)(Raw + 5 * RW + 4 * f);
-                        pv4[0] = p4.x, pv4[1] = p4.y, pv4[2] = p4.z, pv4[3] = p4.w;
-                        xv4[0] = x4.x, xv4[1] = x4.y, xv4[2] = x4.z, xv4[3] = x4.w;
-                    }
+                    float so[4], rno[4];
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
-                        const float s = fmaf(beta, sv[k], wv[k]);
-                        const float rn = fmaf(-alpha, s, rv[k]);
-                        const float u = dv[k] * rn;
-                        val[k] = valid[k] ? u : 0.0f;
-                        so[k] = s;
-                        rno[k] = rn;
-                        po[k] = fmaf(beta, pv4[k], dv[k] * rv[k]);
-                        xo[k] = fmaf(alpha, po[k], xv4[k]);
-                        if (own[k]) {
-                            g_ru = fmaf(rn, u, g_ru);
-                            g_rr = fmaf(rn, rn, g_rr);
-                        }
+                        so[k] = fmaf(beta, sv[k], wv[k]);
+                        rno[k] = fmaf(-alpha, so[k], rv[k]);
+                        val[k] = dv[k] * rno[k];
                     }
-                    if (all_own) {
+                    if (own_all) {
+                        const float4 p4 = *(const float4 *)(Raw + 4 * RW + 4 * f);
+                        const float4 x4 = *(const float4 *)(Raw + 5 * RW + 4 * f);
+                        const float pv[4] = {p4.x, p4.y, p4.z, p4.w}, xv[4] = {x4.x, x4.y, x4.z, x4.w};
+                        float po[4], xo[4];
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) {
+                            po[k] = fmaf(beta, pv[k], dv[k] * rv[k]);
+                            xo[k] = fmaf(alpha, po[k], xv[k]);
+                            g_ru = fmaf(rno[k], val[k], g_ru);
+                            g_rr = fmaf(rno[k], rno[k], g_rr);
+                        }
                         *(float4 *)(cp.snew + gw) = make_float4(so[0], so[1], so[2], so[3]);
                         *(float4 *)(cp.rnew + gw) = make_float4(rno[0], rno[1], rno[2], rno[3]);
                         *(float4 *)(cp.p + gw) = make_float4(po[0], po[1], po[2], po[3]);
                         *(float4 *)(cp.xu + gw) = make_float4(xo[0], xo[1], xo[2], xo[3]);
-                    } else if (any_own) {
+                    } else if (!(in_all && own_none)) {
+                        // edge group: word by word
+                        const bool any_own = !own_none;
+                        float pv[4] = {0.0f, 0.0f, 0.0f, 0.0f}, xv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                        if (any_own) {
+                            const float4 p4 = *(const float4 *)(Raw + 4 * RW + 4 * f);
+                            const float4 x4 = *(const float4 *)(Raw + 5 * RW + 4 * f);
+                            pv[0] = p4.x, pv[1] = p4.y, pv[2] = p4.z, pv[3] = p4.w;
+                            xv[0] = x4.x, xv[1] = x4.y, xv[2] = x4.z, xv[3] = x4.w;
+                        }
 #pragma unroll
-                        for (int k = 0; k < 4; ++k)
-                            if (own[k]) {
+                        for (int k = 0; k < 4; ++k) {
+                            const int cw = cw0 + k;
+                            const bool valid = P.pv && cw >= P.lo3 && cw < P.hi3;
+                            const bool own = valid && any_own && cw >= P.olo3 && cw < P.ohi3;
+                            if (!valid) val[k] = 0.0f;
+                            if (own) {
+                                const float po = fmaf(beta, pv[k], dv[k] * rv[k]);
                                 cp.snew[gw + k] = so[k];
                                 cp.rnew[gw + k] = rno[k];
-                                cp.p[gw + k] = po[k];
-                                cp.xu[gw + k] = xo[k];
+                                cp.p[gw + k] = po;
+                                cp.xu[gw + k] = fmaf(alpha, po, xv[k]);
+                                g_ru = fmaf(rno[k], val[k], g_ru);
+                                g_rr = fmaf(rno[k], rno[k], g_rr);
                             }
+                        }
                     }
                 }
-                // scatter into the node layout: chunk word cw = 3 l + c -> Pf[4 l + c]
-                // (cw0 >= -3, so l >= -1; l <= R; both ends are spare slots)
-                int l = (cw0 + 3) / 3 - 1;
-                int c = cw0 - 3 * l;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    Pf[4 * l + c] = val[k];
-                    if (++c == 3) {
-                        c = 0;
-                        ++l;
-                    }
-                }
+                // scatter into the node layout: chunk word cw = 3 l + c -> Pf[4 l + c]; from
+                // the first word's component c0 the next three sit 1 + (c0 == 2), 2 + (c0 != 0)
+                // and 4 floats further (cw0 >= -3, so l >= -1; l <= R; both ends are spare slots)
+                const int l0 = (cw0 + 3) / 3 - 1;
+                const int c0 = cw0 - 3 * l0;
+                float *d0 = Pf + 4 * l0 + c0;
+                d0[0] = val[0];
+                d0[1 + (c0 == 2)] = val[1];
+                d0[2 + (c0 != 0)] = val[2];
+                d0[4] = val[3];
             }
         }
     };
@@ -361,12 +367,14 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
     };
 
     // ---- prologue: node planes xs-1, xs and element plane xs-1 --------------------------
+    // (the raw buffers hold one plane: the second plane's copies go out after the first
+    // plane is combined)
     issue_plane(xs - 1);
+    issue_eplane(xs - 1);
     commit_plane(0, xs - 1);
     issue_plane(xs);
-    issue_eplane(xs - 1);
-    commit_plane(1, xs);
     commit_eplane(0);
+    commit_plane(1, xs);
     __syncthreads();
 
     float acc[EPT][3];
