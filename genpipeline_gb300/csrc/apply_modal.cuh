@@ -366,9 +366,8 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
         return Bdf[2 * ((pt >> 5) * 12 + (cx * 2 + cy) * 3 + c) + (pe >= NT ? 1 : 0)];
     };
 
-    // ---- prologue: node planes xs-1, xs and element plane xs-1 --------------------------
-    // (the raw buffers hold one plane: the second plane's copies go out after the first
-    // plane is combined)
+    // ---- prologue: node planes xs-1, xs and element plane xs-1 (the raw buffers hold one
+    // plane: the second plane's copies go out after the first plane is combined) ----------
     issue_plane(xs - 1);
     issue_eplane(xs - 1);
     commit_plane(0, xs - 1);
@@ -542,7 +541,7 @@ __global__ void __launch_bounds__(NT, 2)
     apply_modal_kernel(ModalGeom G, const float *__restrict__ x, const float *__restrict__ p, float *__restrict__ y,
                        const uint8_t *__restrict__ mask, Law<float> law, const ModalK km, CgArgs ca) {
     extern __shared__ float4 smem4[];
-    __shared__ double sred[32];
+    __shared__ double sred[3 * 32];
     const int tid = threadIdx.x;
     CgPass cp{0.0f, 0.0f, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int it = 0;
@@ -565,9 +564,8 @@ __global__ void __launch_bounds__(NT, 2)
     if (MODE == MODE_CG) {
         const int nblk = gridDim.x * gridDim.y;
         const int bid = blockIdx.x + gridDim.x * blockIdx.y;
-        double bs[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) bs[k] = block_sum((double)sums[k], sred);
+        double bs[3] = {(double)sums[0], (double)sums[1], (double)sums[2]};
+        block_sum_n<3>(bs, sred);
         __shared__ bool last;
         if (tid == 0) {
 #pragma unroll
@@ -578,13 +576,11 @@ __global__ void __launch_bounds__(NT, 2)
         __syncthreads();
         if (last) {
             __threadfence();
-            double tot[3];
+            double tot[3] = {0.0, 0.0, 0.0};
+            for (int b = tid; b < nblk; b += NT)
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                double s = 0.0;
-                for (int b = tid; b < nblk; b += NT) s += ((volatile double *)ca.partials)[k * nblk + b];
-                tot[k] = block_sum(s, sred);
-            }
+                for (int k = 0; k < 3; ++k) tot[k] += __ldcg(&ca.partials[k * nblk + b]);
+            block_sum_n<3>(tot, sred);
             if (tid == 0) {
                 PcgScalars *sc = ca.sc;
                 sc->counter = 0;

@@ -121,6 +121,31 @@ __device__ __forceinline__ double block_sum(double v, double *scratch) {
     return r;
 }
 
+// K block sums at once, with one pair of barriers (each value follows the tree of
+// block_sum, so the results are the same); valid in thread 0. scratch: 32 K doubles.
+template <int K>
+__device__ __forceinline__ void block_sum_n(double (&v)[K], double *scratch) {
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int lane = tid & 31, warp = tid >> 5;
+    const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) scratch[32 * k + warp] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double r = 0.0;
+        if (warp == 0) {
+            r = lane < nw ? scratch[32 * k + lane] : 0.0;
+            r = warp_sum(r);
+        }
+        v[k] = r;
+    }
+}
+
 constexpr int kModalNnz = 45;
 
 // Modal form of the isotropic cube element (see apply_modal.cuh). Sparsity pattern of Km in (mode*3 + component) indices (derived from the quadrature

@@ -365,10 +365,10 @@ template <int K>
 __device__ bool grid_sums(const double (&v)[K], double *partials, int slot, unsigned *count, unsigned target, int nblk,
                           int bid, unsigned long long wait_ns, double *sred, double (&tot)[K]) {
     __shared__ bool s_ok;
-    __shared__ double s_tot[K];
     double bs[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) bs[k] = block_sum(v[k], sred);
+    for (int k = 0; k < K; ++k) bs[k] = v[k];
+    block_sum_n<K>(bs, sred);
     double *part = partials + (size_t)slot * K * nblk;
     if (threadIdx.x == 0) {
 #pragma unroll
@@ -388,13 +388,17 @@ __device__ bool grid_sums(const double (&v)[K], double *partials, int slot, unsi
     }
     __syncthreads();
     if (!s_ok) return false;
+    double s[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-        double s = 0.0;
-        for (int i = threadIdx.x; i < nblk; i += blockDim.x) s += __ldcg(&part[k * nblk + i]);
-        s = block_sum(s, sred);
-        if (threadIdx.x == 0) s_tot[k] = s;
-    }
+    for (int k = 0; k < K; ++k) s[k] = 0.0;
+    for (int i = threadIdx.x; i < nblk; i += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < K; ++k) s[k] += __ldcg(&part[k * nblk + i]);
+    block_sum_n<K>(s, sred);
+    __shared__ double s_tot[K];
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) s_tot[k] = s[k];
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < K; ++k) tot[k] = s_tot[k];
@@ -422,7 +426,7 @@ __global__ void __launch_bounds__(NT, 2)
     pcg_fused_kernel(const __grid_constant__ FusedTable T, Law<float> law, const ModalK km,
                      unsigned long long wait_ns) {
     extern __shared__ float4 smem4[];
-    __shared__ double sred[32];
+    __shared__ double sred[3 * 32];
     int di = 0;
     while (di + 1 < T.n && (int)blockIdx.x >= T.d[di + 1].block0) ++di;
     const FusedDesign &D = T.d[di];
