@@ -26,7 +26,7 @@ class FEMDesign:
     """One forward solve: densities, load vector and fixed DOFs on a grid (host or device)."""
 
     grid: tuple
-    x: np.ndarray
+    x: object  # (n_elem,) densities: numpy, or a float32 device tensor
     f: np.ndarray
     fixed_dofs: np.ndarray
     u0: Optional[torch.Tensor] = None  # warm start (FP64, device)
@@ -62,7 +62,10 @@ class BatchFEM:
     def upload(self, d: FEMDesign) -> FEMDesign:
         dev = self.eng.device
         nx, ny, nz = d.grid
-        d.dx = torch.as_tensor(np.asarray(d.x, dtype=np.float32).reshape(-1), device=dev).contiguous()
+        if isinstance(d.x, torch.Tensor):  # densities already on the device (e.g. from gbsimp_voxel_prep)
+            d.dx = d.x.reshape(-1).to(device=dev, dtype=torch.float32).contiguous()
+        else:
+            d.dx = torch.as_tensor(np.asarray(d.x, dtype=np.float32).reshape(-1), device=dev).contiguous()
         d.df = torch.as_tensor(np.asarray(d.f, dtype=np.float64), device=dev).contiguous()
         d.dmask = torch.as_tensor(B.node_mask(nx, ny, nz, d.fixed_dofs), device=dev)
         if d.u0 is not None:

@@ -44,3 +44,39 @@ def load_case(name: str, n: int):
     if name == "torsion":
         return bcs.torsion_couple(n, n, n)
     raise ValueError(name)
+
+
+def _grf_field(shape, seed: int, length_scale: float) -> np.ndarray:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    w = rng.standard_normal(shape)
+    k = [np.fft.fftfreq(n) for n in shape]
+    kx, ky, kz = np.meshgrid(*k, indexing="ij")
+    g = np.exp(-2.0 * np.pi ** 2 * length_scale ** 2 * (kx ** 2 + ky ** 2 + kz ** 2))
+    z = np.real(np.fft.ifftn(np.fft.fftn(w) * g))
+    return (z - z.mean()) / (z.std() + 1e-30)
+
+
+class LatentFieldDecoder:
+    """A stand-in for the VAE decoder that the evaluator calls (the VAE itself is not part of
+    this package): ``decode(z)`` maps latent vectors (B, latent_dim) to densities
+    (B, 1, size, size, size) = sigmoid(gain * sum_k z_k F_k), where F_k are fixed seeded
+    Gaussian random fields (``_grf_field`` with PCG64(seed + k)). Deterministic, on the
+    device, with the ``parameters()`` / ``decode`` interface the evaluator uses."""
+
+    def __init__(self, latent_dim: int = 16, size: int = 64, seed: int = 0, length_scale: float = 6.0,
+                 gain: float = 1.5, device="cuda"):
+        import torch
+
+        f = np.stack([_grf_field((size, size, size), seed + k, length_scale) for k in range(latent_dim)])
+        self.fields = torch.as_tensor(f.reshape(latent_dim, -1), dtype=torch.float32, device=device)
+        self.latent_dim, self.size, self.gain = latent_dim, size, gain
+
+    def parameters(self):
+        return iter([self.fields])
+
+    def decode(self, z):
+        import torch
+
+        z = torch.as_tensor(z, dtype=torch.float32, device=self.fields.device).reshape(-1, self.latent_dim)
+        v = torch.sigmoid(self.gain * (z @ self.fields) / np.sqrt(self.latent_dim))
+        return v.reshape(-1, 1, self.size, self.size, self.size)

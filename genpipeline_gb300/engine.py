@@ -277,6 +277,25 @@ class Engine:
                                             _p(x), _p(fixed), nf, C.byref(o), C.byref(st), _p(ws), nb, _stream()))
         return st.as_dict()
 
+    def voxel_prep(self, vol: torch.Tensor, shape_out, sigma: float = 0.5, sharpness: float = 15.0,
+                   out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """(B, D, H, W) or (D, H, W) FP32 device grids -> linear resampling to ``shape_out`` +
+        smooth_voxels (gbsimp_voxel_prep)."""
+        v = vol if vol.dim() == 4 else vol.unsqueeze(0)
+        if v.dtype != torch.float32 or not v.is_cuda or not v.is_contiguous():
+            raise ValueError("voxel_prep: vol must be a contiguous float32 CUDA tensor")
+        b, dd, hh, ww = v.shape
+        d, h, w = (int(n) for n in shape_out)
+        nb = int(self.lib.gbsimp_voxel_prep_ws_bytes(b, dd, hh, ww, d, h, w))
+        if nb == 0:
+            raise ValueError(f"voxel_prep: unsupported extents {tuple(v.shape)} -> {(d, h, w)}")
+        o = torch.empty((b, d, h, w), dtype=torch.float32, device=v.device) if out is None else out
+        _need(o, torch.float32, b * d * h * w, "out")
+        ws = self.workspace("voxel", nb)
+        L.check(self.lib.gbsimp_voxel_prep(self.ctx, b, dd, hh, ww, _p(v), d, h, w, _p(o), float(sigma),
+                                           float(sharpness), _p(ws), nb, _stream()))
+        return o if vol.dim() == 4 else o[0]
+
     def dot64(self, a: torch.Tensor, b: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         _need(a, torch.float64, a.numel(), "a")
         _need(b, torch.float64, a.numel(), "b")

@@ -261,6 +261,21 @@ int gbsimp_pcg_csr_f32(gbsimp_ctx *ctx, int64_t n, const int32_t *row_ptr,
 int gbsimp_dot_f64(gbsimp_ctx *ctx, int64_t n, const double *a, const double *b,
                    double *out, void *ws, size_t ws_bytes, void *stream);
 
+/* ---- evaluator input step ------------------------------------------------------------ */
+/* A batch of (D, H, W) FP32 density grids -> (d, h, w): linear resampling as
+ * scipy.ndimage.zoom(v, zoom, order=1) (output o reads input coordinate
+ * o (n_in - 1) / (n_out - 1)), then smooth_voxels: Gaussian of `sigma` voxels (radius
+ * int(4 sigma + 0.5), mirror "reflect" boundary) and the logistic
+ * 1 / (1 + exp(-sharpness (v - 0.5))). Replaces the host-side zoom + smooth_voxels of
+ * VoxelFEMEvaluator.evaluate (fem/voxel_fem.py:457-462, pipeline_utils.py:55-76); d = D etc.
+ * gives smooth_voxels alone. Extents 1..1024 (an output extent of 1 only for an input
+ * extent of 1); returns GBS_EINVAL when a row of the combined filter needs more than 32 taps.
+ * Returns 0 from the size query for invalid extents. */
+size_t gbsimp_voxel_prep_ws_bytes(int batch, int D, int H, int W, int d, int h, int w);
+int gbsimp_voxel_prep(gbsimp_ctx *ctx, int batch, int D, int H, int W, const float *in, int d,
+                      int h, int w, float *out, double sigma, double sharpness, void *ws,
+                      size_t ws_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

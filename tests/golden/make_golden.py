@@ -23,6 +23,11 @@ Recorded (all FP64):
                         with the SPD stiffness injected.
 * ``simp_c0.npz``       (``--c0``, ~7 min) the 32x16x16, volfrac 0.3, rmin 1.5, penal 3,
                         50-iteration ``SIMPSolver.run`` with the SPD stiffness injected.
+* ``voxel.npz``         the evaluator's input step as ``VoxelFEMEvaluator.evaluate`` runs
+                        it (``genpipeline/fem/voxel_fem.py:457-462``):
+                        ``scipy.ndimage.zoom(v, zoom, order=1)`` then the reference's
+                        ``pipeline_utils.smooth_voxels`` (``:55-76``), on float32 grids
+                        (the decoder's dtype). Inputs are seeded ``PCG64`` uniforms.
 """
 from __future__ import annotations
 
@@ -291,13 +296,48 @@ def make_c0(ss, out):
     print(f"C0: compliance {s.last_compliance:.10f} in {dt:.1f} s")
 
 
+VOXEL_CASES = [  # (name, input shape, seed, zoom)
+    ("z16", (16, 16, 16), 1, 0.5),
+    ("z64", (64, 64, 64), 2, 0.5),
+    ("s_only", (12, 10, 9), 3, 1.0),
+    ("z_odd", (20, 17, 9), 4, 0.5),
+]
+
+
+def voxel_input(shape, seed) -> np.ndarray:
+    return np.random.Generator(np.random.PCG64(seed)).random(shape, dtype=np.float32)
+
+
+def make_voxel(path):
+    from scipy.ndimage import zoom
+
+    from genpipeline.pipeline_utils import smooth_voxels
+
+    out = {}
+    for name, shape, seed, z in VOXEL_CASES:
+        v = voxel_input(shape, seed)
+        if z != 1.0:
+            v = zoom(v, z, order=1)
+        r = smooth_voxels(v)
+        out[f"{name}_out"] = np.asarray(r, dtype=np.float32)
+        if int(np.prod(shape)) <= 16 ** 3:
+            out[f"{name}_in"] = voxel_input(shape, seed)
+    np.savez_compressed(path, **out)
+    print("wrote", path, {k: v.shape for k, v in out.items()})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--c0", action="store_true", help="also run the 50-iteration 32x16x16 case")
     ap.add_argument("--only-c0", action="store_true")
+    ap.add_argument("--only-voxel", action="store_true", help="only the evaluator input step fixtures")
     a = ap.parse_args()
     ss = _import_reference(a.reference)
+    if a.only_voxel:
+        make_voxel(os.path.join(HERE, "voxel.npz"))
+        return
+    make_voxel(os.path.join(HERE, "voxel.npz"))
     if not a.only_c0:
         make_ke(ss, os.path.join(HERE, "ke.npz"))
         make_kernels(ss, os.path.join(HERE, "kernels.npz"))
