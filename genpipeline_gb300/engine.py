@@ -296,6 +296,27 @@ class Engine:
                                            float(sharpness), _p(ws), nb, _stream()))
         return o if vol.dim() == 4 else o[0]
 
+    def marching_cubes(self, vol: torch.Tensor, level: float, spacing=(1.0, 1.0, 1.0)) -> torch.Tensor:
+        """(n_tri, 3, 3) FP32 triangles of the isosurface of a (nx, ny, nz) FP32 device grid
+        (gbsimp_marching_cubes; two calls: count, then emit)."""
+        if vol.dim() != 3 or vol.dtype != torch.float32 or not vol.is_cuda or not vol.is_contiguous():
+            raise ValueError("marching_cubes: vol must be a contiguous (nx, ny, nz) float32 CUDA tensor")
+        nx, ny, nz = vol.shape
+        nb = int(self.lib.gbsimp_marching_cubes_ws_bytes(nx, ny, nz))
+        if nb == 0:
+            raise ValueError("marching_cubes: every extent must be >= 2")
+        ws = self.workspace("mc", nb)
+        n = C.c_int64(0)
+        sx, sy, sz = (float(s) for s in spacing)
+        L.check(self.lib.gbsimp_marching_cubes(self.ctx, nx, ny, nz, _p(vol), float(level), sx, sy, sz, None, 0,
+                                               C.byref(n), _p(ws), nb, _stream()))
+        out = torch.empty((max(int(n.value), 0), 3, 3), dtype=torch.float32, device=vol.device)
+        if n.value > 0:
+            m = C.c_int64(0)
+            L.check(self.lib.gbsimp_marching_cubes(self.ctx, nx, ny, nz, _p(vol), float(level), sx, sy, sz,
+                                                   _p(out), out.shape[0], C.byref(m), _p(ws), nb, _stream()))
+        return out
+
     def dot64(self, a: torch.Tensor, b: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         _need(a, torch.float64, a.numel(), "a")
         _need(b, torch.float64, a.numel(), "b")

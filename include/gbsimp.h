@@ -276,6 +276,24 @@ int gbsimp_voxel_prep(gbsimp_ctx *ctx, int batch, int D, int H, int W, const flo
                       int h, int w, float *out, double sigma, double sharpness, void *ws,
                       size_t ws_bytes, void *stream);
 
+/* ---- STL export step ------------------------------------------------------------------- */
+/* Isosurface of an (nx, ny, nz) FP32 grid (C order) at `level`: marching cubes over the cells
+ * between grid points, as density_to_stl extracts it before writing the STL
+ * (topology/mesh_export.py:7-67, which uses skimage on the host). Corners with
+ * value >= level are inside; ambiguous faces separate their inside corners (no cracks);
+ * triangles point from inside to outside. Output: 9 floats per triangle (three vertices in
+ * grid units times (sx, sy, sz)), in cell order. *n_tris receives the count; when tris is
+ * NULL or max_tris < count nothing is written (size query). Synchronises the stream. */
+size_t gbsimp_marching_cubes_ws_bytes(int nx, int ny, int nz);
+int gbsimp_marching_cubes(gbsimp_ctx *ctx, int nx, int ny, int nz, const float *vol, double level,
+                          double sx, double sy, double sz, float *tris, int64_t max_tris,
+                          int64_t *n_tris, void *ws, size_t ws_bytes, void *stream);
+/* The case table the kernel uses (host memory, no GPU needed): per case the triangle count
+ * (ntri[256]), loop count (nloop[256]), loop lengths (len[256][4]) and the loops' cut-edge
+ * indices (edge[256][12]). Any pointer may be NULL. Returns the largest triangle count. */
+int gbsimp_marching_cubes_table(unsigned char *ntri, unsigned char *nloop, unsigned char *len,
+                                signed char *edge);
+
 #ifdef __cplusplus
 }
 #endif
