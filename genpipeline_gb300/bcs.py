@@ -122,21 +122,14 @@ def _face_gpu_load(lf, ix, iy, iz, nx, ny, nz):
     return table.get(lf, ix == nx) if isinstance(lf, str) else ix == nx
 
 
-def reference_gpu(nx, ny, nz, bcs=None, force_mag=1.0):
-    """Fixed DOFs and load vector of SIMPSolverGPU._get_bcs (simp_solver_gpu.py:138-311)."""
-    b = {"fixed_face": "x_min", "load_face": "x_max", "load_dof": 2}
-    if bcs:
-        b.update(bcs)
+def _gpu_pattern_load(nx, ny, nz, b, force_mag, fixed_nodes):
+    """The named-position and grid loads of SIMPSolverGPU (simp_solver_gpu.py:250-311)."""
     ix, iy, iz = _grid(nx, ny, nz)
     ids = (ix * (ny + 1) + iy) * (nz + 1) + iz
-    fixed_nodes = ids[_face_gpu_fixed(b.get("fixed_face", "x_min"), ix, iy, iz, nx, ny, nz)]
     f = np.zeros(3 * n_nodes(nx, ny, nz))
-    lf = b.get("load_face", "x_max")
     ld = b.get("load_dof", 2)
-    multi = b.get("multi_load", False)
     positions = b.get("load_positions", None)
-    pattern = b.get("load_pattern", None)
-    if multi and positions:
+    if positions:
         # _apply_multi_position_load (:250-292): position masks over the whole grid.
         for pos in positions:
             if pos == "top":
@@ -155,18 +148,49 @@ def reference_gpu(nx, ny, nz, bcs=None, force_mag=1.0):
                 fpn = float(force_mag) / len(positions)
                 for node in v[:: max(1, len(v) // 3)]:
                     f[3 * node + ld] -= fpn
-        return f, _fixed_dofs(fixed_nodes)
-    if multi and pattern == "grid":
-        # _apply_grid_load (:294-311): rows of constant z every max(1, nz//4).
-        spacing = max(1, nz // 4)
-        for zv in range(0, nz + 1, spacing):
-            nodes = ids[iz == zv]
-            v = nodes[~np.isin(nodes, fixed_nodes)]
-            if len(v) > 0:
-                fpn = float(force_mag) / ((nz // spacing) + 1)
-                for node in v[:: max(1, len(v) // 2)]:
-                    f[3 * node + ld] -= fpn
-        return f, _fixed_dofs(fixed_nodes)
+        return f
+    # _apply_grid_load (:294-311): rows of constant z every max(1, nz//4).
+    spacing = max(1, nz // 4)
+    for zv in range(0, nz + 1, spacing):
+        nodes = ids[iz == zv]
+        v = nodes[~np.isin(nodes, fixed_nodes)]
+        if len(v) > 0:
+            fpn = float(force_mag) / ((nz // spacing) + 1)
+            for node in v[:: max(1, len(v) // 2)]:
+                f[3 * node + ld] -= fpn
+    return f
+
+
+def generator(nx, ny, nz, bcs=None, force_mag=1.0):
+    """Boundary conditions of the data generator's geometries (topo_data_gen.py:41-95): the
+    clamped faces and loads of SIMPSolver._get_bcs (simp_solver.py:81-157), which accepts
+    lists of faces and of load directions; a named-position or grid load (multi_load with
+    load_positions / load_pattern), which only SIMPSolverGPU implements
+    (simp_solver_gpu.py:250-311), is spread as that class spreads it, over the nodes that the
+    clamped faces leave free."""
+    b = {"fixed_face": "x_min", "load_face": "x_max", "load_dof": 2}
+    if bcs:
+        b.update(bcs)
+    f, fixed = reference_cpu(nx, ny, nz, b, force_mag)
+    if b.get("multi_load") and (b.get("load_positions") or b.get("load_pattern") == "grid"):
+        f = _gpu_pattern_load(nx, ny, nz, b, force_mag, np.unique(fixed // 3))
+    return f, fixed
+
+
+def reference_gpu(nx, ny, nz, bcs=None, force_mag=1.0):
+    """Fixed DOFs and load vector of SIMPSolverGPU._get_bcs (simp_solver_gpu.py:138-311)."""
+    b = {"fixed_face": "x_min", "load_face": "x_max", "load_dof": 2}
+    if bcs:
+        b.update(bcs)
+    ix, iy, iz = _grid(nx, ny, nz)
+    ids = (ix * (ny + 1) + iy) * (nz + 1) + iz
+    fixed_nodes = ids[_face_gpu_fixed(b.get("fixed_face", "x_min"), ix, iy, iz, nx, ny, nz)]
+    f = np.zeros(3 * n_nodes(nx, ny, nz))
+    lf = b.get("load_face", "x_max")
+    ld = b.get("load_dof", 2)
+    multi = b.get("multi_load", False)
+    if multi and (b.get("load_positions") or b.get("load_pattern") == "grid"):
+        return _gpu_pattern_load(nx, ny, nz, b, force_mag, fixed_nodes), _fixed_dofs(fixed_nodes)
     nodes = ids[_face_gpu_load(lf, ix, iy, iz, nx, ny, nz)]
     if len(nodes) > 0:
         v = nodes[~np.isin(nodes, fixed_nodes)]

@@ -26,6 +26,7 @@ import torch
 from .. import _lib as L
 from .. import bcs as B
 from ..engine import Engine, get_engine, n_dof, n_elem
+from .batch_simp import reference_schedule
 
 
 @dataclass
@@ -44,6 +45,8 @@ class MatrixFreeK:
 
 class SIMPSolverGPU:
     _RESOURCE_CACHE = {}
+    # (tol, max_iter) of the sensitivity solve per iteration (simp_solver_gpu.py:92-99)
+    tol_schedule = staticmethod(reference_schedule)
 
     def __init__(self, nx: int = 32, ny: int = 8, nz: int = 8, penal: float = 3.0, rmin: float = 1.5,
                  boundary_conditions: dict | None = None, device: str = "cuda",
@@ -154,12 +157,7 @@ class SIMPSolverGPU:
         change = 0.0
         curr = float("nan")
         for i in range(n_iters):
-            if i < 3:
-                tol, max_iter = 1e-4, 200
-            elif i < 8:
-                tol, max_iter = 1e-5, 400
-            else:
-                tol, max_iter = 1e-6, 800
+            tol, max_iter = self.tol_schedule(i)
             dc = self._sensitivity(xPhys, force_mag, tol=tol, max_iter=max_iter)
             if torch.isnan(dc).any():
                 print(f"  [SIMP-GPU] FATAL: NaN in sensitivity at iter {i}")
