@@ -64,6 +64,8 @@ def _args():
     ap.add_argument("--cpu-sample-steps", type=int, default=1)
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched FEM (served vs plain) measurement")
+    ap.add_argument("--no-rows", action="store_true",
+                    help="skip the evaluator / STL / generator measurements")
     ap.add_argument("--host-loop", action="store_true",
                     help="launch PCG iterations from the host (for kernel profilers) instead of the graph loop")
     return ap.parse_args()
@@ -237,6 +239,109 @@ def measure_batch(repeats=2):
             "unit": "FEM solves/s"}
 
 
+# ---- the rows next to the path: evaluator input step, evaluator, STL export, generator -----
+def _cuda_time(fn, reps=5):
+    import torch
+
+    fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    e.synchronize()
+    return s.elapsed_time(e) * 1e-3 / reps
+
+
+def measure_rows(xphys64=None):
+    """Short measurements of the evaluator input step, the served evaluator, the STL surface and
+    the batched data generator (each a few seconds)."""
+    import numpy as np
+    import torch
+
+    from genpipeline_gb300.designs import LatentFieldDecoder
+    from genpipeline_gb300.engine import get_engine
+    from genpipeline_gb300.fem.voxel_fem import VoxelFEMEvaluator
+    from genpipeline_gb300.schema import DesignParameters
+
+    eng = get_engine()
+    rows = {}
+    # evaluator input step: 16 x 64^3 -> 32^3 (zoom 0.5 + smooth_voxels)
+    vols = torch.rand((16, 64, 64, 64), device="cuda")
+    t = _cuda_time(lambda: eng.voxel_prep(vols, (32, 32, 32)))
+    nbytes = 4 * (16 * 64 ** 3 + 16 * 32 ** 3)
+    cpu = None
+    try:
+        from scipy.ndimage import gaussian_filter, zoom
+
+        v0 = vols[0].cpu().numpy()
+        c0 = time.perf_counter()
+        z = zoom(v0, 0.5, order=1)
+        _ = 1.0 / (1.0 + np.exp(-15.0 * (gaussian_filter(z, sigma=0.5) - 0.5)))
+        cpu = {"value": 1.0 / (time.perf_counter() - c0), "unit": "grids/s", "cores": 1,
+               "kind": "reference", "sample": "one 64^3 grid: scipy zoom(order=1) + the smooth_voxels steps"}
+    except ImportError:
+        pass
+    rows["voxel_prep"] = {"workload": "16 x 64^3 -> 32^3 (zoom 0.5, Gaussian 0.5, logistic 15)",
+                          "value": 16 / t, "unit": "grids/s", "ms_per_batch": t * 1e3,
+                          "algorithmic_GBs": nbytes / t / 1e9, "cpu_baseline": cpu}
+    # served evaluator vs one evaluation at a time (stand-in decoder, 16 latents)
+    dec = LatentFieldDecoder(latent_dim=16, size=64, seed=3)
+    rng = np.random.Generator(np.random.PCG64(4))
+    params = [DesignParameters(h_mm=10.0, r_mm=2.0, latent_z=list(rng.standard_normal(16))) for _ in range(16)]
+    ev = VoxelFEMEvaluator(use_gpu=True, vae_model=dec)
+    ev.evaluate_batch(params[:2])
+    torch.cuda.synchronize()
+    c0 = time.perf_counter()
+    served = ev.evaluate_batch(params)
+    torch.cuda.synchronize()
+    ts = time.perf_counter() - c0
+    c0 = time.perf_counter()
+    plain = [ev.evaluate(np.asarray(p.latent_z), dec) for p in params]
+    torch.cuda.synchronize()
+    tp = time.perf_counter() - c0
+    diff = max(abs(s.compliance - p["compliance"]) / abs(p["compliance"]) for s, p in zip(served, plain))
+    rows["evaluator"] = {"workload": "16 latents: decode (stand-in) + 64^3->32^3 prep + GPUVoxelFEM solve "
+                                     "(penal 1, x_min clamped, 1000 N on x_max) to rtol 1e-8",
+                         "served": 16 / ts, "plain": 16 / tp, "served_over_plain": tp / ts, "unit": "evaluations/s",
+                         "max_compliance_rel_diff": diff}
+    # STL surface of the benchmark's 64^3 design
+    x = xphys64 if xphys64 is not None else torch.rand((64, 64, 64), device="cuda")
+    x = x.reshape(64, 64, 64).contiguous()
+    ntri = eng.marching_cubes(x, 0.5).shape[0]
+    t = _cuda_time(lambda: eng.marching_cubes(x, 0.5))
+    rows["stl_surface"] = {"workload": "isosurface at 0.5 of the 64^3 design (marching cubes, count + emit)",
+                           "value": 63 ** 3 / t / 1e9, "unit": "Gcells/s", "ms": t * 1e3, "triangles": ntri}
+    # batched SIMP generator vs one solver per sample
+    from genpipeline_gb300 import bcs as B
+    from genpipeline_gb300.topology.batch_simp import BatchSIMP
+    from genpipeline_gb300.topology.simp_solver_gpu import SIMPSolverGPU
+    from genpipeline_gb300.topology.topo_data_gen import TopoDataGenerator
+
+    np.random.seed(11)
+    gen = TopoDataGenerator(output_dir=os.path.join("/tmp", "gb_rows_gen"), n_iters=10)
+    cases = [gen._draw() for _ in range(16)]
+    BatchSIMP(cases[:2], bc_fn=B.generator).run(2)
+    torch.cuda.synchronize()
+    c0 = time.perf_counter()
+    BatchSIMP(cases, bc_fn=B.generator).run(10)
+    torch.cuda.synchronize()
+    tb = time.perf_counter() - c0
+    simple = [c for c in cases if not isinstance(c.bcs.get("load_dof"), list)
+              and not isinstance(c.bcs.get("fixed_face"), list)][:4]
+    c0 = time.perf_counter()
+    for c in simple:
+        SIMPSolverGPU(nx=c.grid[0], ny=c.grid[1], nz=c.grid[2], penal=c.penal, rmin=c.rmin,
+                      boundary_conditions=c.bcs).run(volfrac=c.volfrac, n_iters=10, force_mag=c.force_mag)
+    torch.cuda.synchronize()
+    tsq = (time.perf_counter() - c0) / max(len(simple), 1)
+    rows["generator"] = {"workload": "16 generator samples (medium grids, GEOM_BCS), 10 SIMP iterations each",
+                         "batched": 16 / tb, "one_solver_per_sample": 1.0 / tsq,
+                         "batched_over_one": (16 / tb) * tsq, "unit": "samples/s"}
+    return rows
+
+
 def run_serve(a):
     """Serving stream: Poisson arrivals at 200/s, edge U{24,32,48,64,96}, three load cases,
     ~10% repeated designs; continuous batching with admission by free HBM."""
@@ -405,8 +510,11 @@ def run_ours(a):
                "seconds": tc}
 
     fem = None
+    rows = None
     if rank == 0 and a.workload == "simp64" and not a.no_batch:
         fem = measure_batch()
+    if rank == 0 and a.workload == "simp64" and not a.no_rows:
+        rows = measure_rows(prob.xphys)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
@@ -418,7 +526,7 @@ def run_ours(a):
                                parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clk, "pcg_iterations_per_step": pcg_iters / a.steps,
-                "compliance_rel_err_vs_fp64_oracle": rel_err, "fem_solves_per_s": fem}
+                "compliance_rel_err_vs_fp64_oracle": rel_err, "fem_solves_per_s": fem, "next_rows": rows}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
