@@ -119,6 +119,8 @@ SIGNATURES = {
     "gbsimp_dot_f64": (_I, [_P, _I64, _P, _P, _P, _P, _SZ, _P]),
     "gbsimp_voxel_prep_ws_bytes": (_SZ, [_I, _I, _I, _I, _I, _I, _I]),
     "gbsimp_voxel_prep": (_I, [_P, _I, _I, _I, _I, _P, _I, _I, _I, _P, _D, _D, _P, _SZ, _P]),
+    "gbsimp_barrier_selftest_ws_bytes": (_SZ, []),
+    "gbsimp_barrier_selftest": (_I, [_P, _I, _D, C.POINTER(C.c_int), _P, _SZ, _P]),
     "gbsimp_marching_cubes_ws_bytes": (_SZ, [_I, _I, _I]),
     "gbsimp_marching_cubes_table": (_I, [_P, _P, _P, _P]),
     "gbsimp_marching_cubes": (_I, [_P, _I, _I, _I, _P, _D, _D, _D, _D, _P, _I64, C.POINTER(C.c_int64), _P, _SZ,

@@ -405,6 +405,23 @@ __device__ bool grid_sums(const double (&v)[K], double *partials, int slot, unsi
     return true;
 }
 
+// Self-test of the grid barrier above: every block arrives once and waits for
+// gridDim.x + extra arrivals. With extra = 0 the barrier completes and every block sums the
+// partials (one per block, 1.0 each); with extra > 0 nothing ever supplies the missing
+// arrivals, so each block's bounded wait expires and the kernel records GBS_ETIMEOUT.
+__global__ void barrier_selftest_kernel(double *partials, unsigned *count, int *status, unsigned extra,
+                                        unsigned long long wait_ns) {
+    __shared__ double sred[32];
+    const double v[1] = {threadIdx.x == 0 ? 1.0 : 0.0};  // 1.0 per block
+    double tot[1];
+    const bool ok = grid_sums<1>(v, partials, 0, count, gridDim.x + extra, (int)gridDim.x, (int)blockIdx.x, wait_ns,
+                                 sred, tot);
+    if (threadIdx.x == 0) {
+        if (!ok) atomicExch(status, (int)GBS_ETIMEOUT);
+        else if (tot[0] != (double)gridDim.x) atomicExch(status, (int)GBS_EINVAL);
+    }
+}
+
 // Designs of one cooperative launch. Each design owns the CTA range [block0, block0 + nblk)
 // laid out as `tiles` flat tiles x (nblk / tiles) x segments, its own PCG state and barrier
 // counter; designs advance independently.
@@ -1539,5 +1556,42 @@ extern "C" int gbsimp_batch_solve(gbsimp_ctx *ctx, gbsimp_batch_item *items, int
             items[i].state = 2;
             items[i].stats.status = GBS_ENOTCONV;
         }
+    return GBS_OK;
+}
+
+extern "C" size_t gbsimp_barrier_selftest_ws_bytes(void) { return 256 + 4096 * sizeof(double) + 256; }
+
+extern "C" int gbsimp_barrier_selftest(gbsimp_ctx *ctx, int extra_arrivals, double wait_seconds, int *status_out,
+                                       void *ws, size_t ws_bytes, void *stream) {
+    if (!ctx || !status_out || !ws || extra_arrivals < 0 || extra_arrivals > 1024 || !(wait_seconds > 0.0) ||
+        wait_seconds > 2.0 || ws_bytes < gbsimp_barrier_selftest_ws_bytes())
+        return set_error(GBS_EINVAL, "gbsimp_barrier_selftest: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    char *p = align256(ws);
+    unsigned *count = (unsigned *)p;
+    int *status = (int *)(p + 64);
+    double *partials = (double *)(p + 256);
+    GBS_CUDA_TRY(cudaMemsetAsync(p, 0, 256, st));
+    int coop = 0, per_sm = 0;
+    GBS_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
+    GBS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, barrier_selftest_kernel, 128, 0));
+    if (!coop || per_sm < 1) return set_error(GBS_EINVAL, "gbsimp_barrier_selftest: no cooperative launch");
+    int nblk = ctx->num_sms > 0 ? ctx->num_sms : 1;  // one block per SM: all co-resident
+    if (nblk > 4096) nblk = 4096;
+    unsigned extra = (unsigned)extra_arrivals;
+    unsigned long long wait_ns = (unsigned long long)(wait_seconds * 1e9);
+    void *args[] = {&partials, &count, &status, &extra, &wait_ns};
+    const cudaError_t e =
+        cudaLaunchCooperativeKernel((void *)barrier_selftest_kernel, dim3((unsigned)nblk), dim3(128), args, 0, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_error(e, "barrier_selftest_kernel");
+    }
+    count_launches(1);
+    void *hp = thread_pinned();
+    if (!hp) return set_error(GBS_ECUDA, "no pinned staging buffer");
+    GBS_CUDA_TRY(cudaMemcpyAsync(hp, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GBS_CUDA_TRY(cudaStreamSynchronize(st));
+    memcpy(status_out, hp, sizeof(int));
     return GBS_OK;
 }

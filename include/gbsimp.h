@@ -256,6 +256,16 @@ int gbsimp_pcg_csr_f32(gbsimp_ctx *ctx, int64_t n, const int32_t *row_ptr,
                        const gbsimp_solve_opts *opts, gbsimp_solve_stats *stats, void *ws,
                        size_t ws_bytes, void *stream);
 
+/* Diagnostic of the persistent kernels' grid barrier (no counterpart in the reference): one
+ * cooperative launch (one block per SM) in which every block arrives once and waits, at most
+ * wait_seconds (<= 2), for gridDim + extra_arrivals arrivals. *status_out is GBS_OK when the
+ * barrier completed with the right sum (extra_arrivals = 0) and GBS_ETIMEOUT when the bounded
+ * wait expired because the missing arrivals never came (extra_arrivals > 0); the context
+ * stays usable either way. Synchronises the stream. */
+size_t gbsimp_barrier_selftest_ws_bytes(void);
+int gbsimp_barrier_selftest(gbsimp_ctx *ctx, int extra_arrivals, double wait_seconds, int *status_out,
+                            void *ws, size_t ws_bytes, void *stream);
+
 /* ---- reductions used by the host loops -------------------------------------------- */
 /* out (device double) = sum_i a_i * b_i over n FP64 entries, fixed block order. */
 int gbsimp_dot_f64(gbsimp_ctx *ctx, int64_t n, const double *a, const double *b,
