@@ -161,6 +161,23 @@ def _dist():
     return world, rank, local
 
 
+def max_over_ranks(t: float, world: int, device) -> float:
+    """The slowest rank's time (all ranks get it): replicas report N * K / max time."""
+    if world <= 1:
+        return t
+    import torch
+    import torch.distributed as dist
+
+    tt = torch.tensor([t], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def whole_job_rate(world: int, steps: int, t_max: float) -> float:
+    """Units of all replicas (world x steps) over the slowest rank's time."""
+    return world * steps / t_max
+
+
 def _measured_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -425,12 +442,8 @@ def run_ours(a):
     launches = lib.gbsimp_launch_count() - launches0  # our kernels only (the L2 flush is torch)
     clk = clocks.stop()
     t = st0.elapsed_time(st1) * 1e-3
-    tmax = t
-    if world > 1:
-        tt = torch.tensor([t], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        tmax = float(tt.item())
-    value = world * a.steps / tmax
+    tmax = max_over_ranks(t, world, dev)
+    value = whole_job_rate(world, a.steps, tmax)
     pcg_iters = sum(s["iterations"] for s in stats)
     # The dominant kernel, timed live on the final density field of the timed region:
     # 50 back-to-back launches replayed from a CUDA graph, CUDA events on this stream.
@@ -453,12 +466,8 @@ def run_ours(a):
         torch.cuda.current_stream().synchronize()
         x_host, xn_host = xn_host, x_host
     barrier()
-    te = time.perf_counter() - e0
-    if world > 1:
-        tt = torch.tensor([te], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        te = float(tt.item())
-    e2e = {"value": world * a.steps / te, "unit": UNIT, "h2d_bytes_per_step": 4 * ne,
+    te = max_over_ranks(time.perf_counter() - e0, world, dev)
+    e2e = {"value": whole_job_rate(world, a.steps, te), "unit": UNIT, "h2d_bytes_per_step": 4 * ne,
            "d2h_bytes_per_step": 8 * ne}
 
     # ---- roofline of the dominant kernel (the one-kernel PCG iteration) -----------------
