@@ -187,8 +187,9 @@ def _measured_peak():
 
 
 def _profiled_traffic(workload="simp64"):
-    """dram bytes per launch of the PCG apply kernel from the committed ncu summary of the workload."""
-    name = {"simp64": "apply_pcg__simp_64cube.md", "c4": "apply_pcg__simp_192x96x96.md"}.get(workload)
+    """DRAM bytes per launch of the one-kernel PCG iteration from the committed ncu summary of the
+    workload."""
+    name = {"simp64": "cg_iteration__simp_64cube.md", "c4": "cg_iteration__simp_192x96x96.md"}.get(workload)
     if name is None:
         return None
     path = os.path.join(ROOT, "profiles", name)
