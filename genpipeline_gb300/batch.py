@@ -51,7 +51,7 @@ class BatchFEM:
     """Runs gbsimp_batch_round over a changing set of designs."""
 
     def __init__(self, engine: Optional[Engine] = None, law: Optional[L.Law] = None, rtol: float = 1e-8,
-                 inner_rtol: float = 1e-3, max_iter: int = 200000, max_outer: int = 30, fused: bool = True):
+                 inner_rtol: float = 1e-4, max_iter: int = 200000, max_outer: int = 30, fused: bool = True):
         self.eng = engine or get_engine()
         self.law = law or L.make_law("modified", 3.0)
         self.opts = Engine.opts(rtol=rtol, inner_rtol=inner_rtol, max_iter=max_iter, max_outer=max_outer,
@@ -116,7 +116,7 @@ class BatchFEM:
 
 
 def solve_plain(designs: List[FEMDesign], engine: Optional[Engine] = None, law: Optional[L.Law] = None,
-                rtol: float = 1e-8, inner_rtol: float = 1e-3) -> List[FEMDesign]:
+                rtol: float = 1e-8, inner_rtol: float = 1e-4) -> List[FEMDesign]:
     """The one-design-at-a-time form: one gbsimp_solve (graph-loop PCG) per design."""
     eng = engine or get_engine()
     law = law or L.make_law("modified", 3.0)

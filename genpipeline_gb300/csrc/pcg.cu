@@ -961,7 +961,7 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
     int total = 0, outer = 0, status = GBS_OK;
     double relres = 0.0;
     const int max_outer = o->max_outer > 0 ? o->max_outer : 20;
-    const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-3;
+    const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-4;
     for (;;) {
         int rc = ctx->modal_ok ? apply_f64_modal(ctx, nx, ny, nz, law, x, u, w.r64, mask, w.elem, st)
                                : apply_f64(ctx, nx, ny, nz, law, x, u, w.r64, mask, st);
@@ -1386,7 +1386,7 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
                             const gbsimp_solve_opts *o, cudaStream_t st) {
     const Law<float> law = make_law<float>(*glaw);
     const int max_outer = o->max_outer > 0 ? o->max_outer : 20;
-    const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-3;
+    const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-4;
     std::vector<int> act;
     for (int i = 0; i < n; ++i)
         if (items[i].state == 0) act.push_back(i);

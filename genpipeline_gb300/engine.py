@@ -208,7 +208,7 @@ class Engine:
         return lam.value, steps.value
 
     @staticmethod
-    def opts(rtol=1e-8, inner_rtol=1e-3, max_iter=20000, max_outer=20, check_every=0, fused=0,
+    def opts(rtol=1e-8, inner_rtol=1e-4, max_iter=20000, max_outer=20, check_every=0, fused=0,
              profile=0) -> L.SolveOpts:
         return L.SolveOpts(float(rtol), float(inner_rtol), int(max_iter), int(max_outer), int(check_every),
                            int(fused), int(profile), 0)
@@ -242,7 +242,7 @@ class Engine:
         return sec.value
 
     def solve(self, grid: Grid, law: L.Law, x: torch.Tensor, f: torch.Tensor, mask: Optional[torch.Tensor],
-              u: torch.Tensor, rtol=1e-8, inner_rtol=1e-3, max_iter=100000, max_outer=30, check_every=0,
+              u: torch.Tensor, rtol=1e-8, inner_rtol=1e-4, max_iter=100000, max_outer=30, check_every=0,
               key: str = "solve", profile=False, fused=False) -> dict:
         nx, ny, nz = grid
         nd = n_dof(grid)

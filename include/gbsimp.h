@@ -65,7 +65,7 @@ typedef struct gbsimp_oc_params {
 /* Options and results of the linear solves. */
 typedef struct gbsimp_solve_opts {
     double rtol;          /* stop when ||D(f - K u)|| <= rtol * ||D f|| (FP64 residual) */
-    double inner_rtol;    /* FP32 PCG reduction per outer correction (gbsimp_solve only) */
+    double inner_rtol;    /* FP32 PCG reduction per outer correction (gbsimp_solve, batch); <= 0: 1e-4 */
     int32_t max_iter;     /* cap on the total FP32 PCG iterations */
     int32_t max_outer;    /* cap on FP64 defect corrections (gbsimp_solve only) */
     int32_t check_every;  /* iterations between host-side convergence checks (0 = auto) */
