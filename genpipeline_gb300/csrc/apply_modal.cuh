@@ -17,8 +17,9 @@
 // (flat = j*(nz+1) + k) and walks along x. A plane's R = F + 2(nz+2) staged nodes are one
 // contiguous run of 3R words in every node vector, so each staged vector is copied as
 // 16-byte groups with cp.async (no registers held while the copies fly) into a raw buffer,
-// and combined group by group (float4) into the operand plane, laid out as one float4 per
-// node for the element gathers. Per step the CTA computes one plane of elements from two
+// and combined group by group (float4) into the operand plane, laid out as one row per
+// component, so that the element pair of a thread (tid, tid + NT) loads each corner value
+// straight into the two lanes of a packed FP32x2 register. Per step the CTA computes one plane of elements from two
 // operand planes while the copies of the plane after next are in flight. Each element's 24
 // corner contributions are combined along z with a warp shuffle (the element to the left
 // is the lane to the left), along y through a 6-float shared slot per element, and along x
@@ -37,7 +38,8 @@ struct ModalGeom {
 
 
 // Shared memory of the modal kernel for a given z extent (NT = 256, EPT = 2): three operand
-// planes of R + 2 float4 nodes, the raw cp.async buffers (one per staged vector: p for the
+// planes of three component rows of R + 2 floats (rounded up to a multiple of 4), the raw
+// cp.async buffers (one per staged vector: p for the
 // plain apply; r, w, s, 1/diag, p, x for the PCG modes) and the output words of a plane,
 // each 4 * ceil((3R + 3) / 4) floats, two planes of element moduli, the y-direction slots
 // (6 floats per element) and the warp-boundary contributions (12 floats per warp and lane).
@@ -45,7 +47,8 @@ template <int NT, int EPT>
 inline size_t modal_smem_bytes(int nz, bool cg) {
     const int NE = NT * EPT, H = nz + 2, R = NE + H;
     const size_t RW = 4 * (size_t)((3 * R + 6) / 4);
-    return 3 * (size_t)(R + 2) * sizeof(float4) + ((cg ? 6 : 1) + 1) * RW * sizeof(float) +
+    const size_t PR = 4 * (size_t)((R + 5) / 4);
+    return 9 * PR * sizeof(float) + ((cg ? 6 : 1) + 1) * RW * sizeof(float) +
            (2 + 6) * (size_t)NT * sizeof(float2) + (size_t)(NT / 32) * 12 * sizeof(float2);
 }
 
@@ -182,8 +185,9 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
     const int RW = 4 * ((3 * R + 6) / 4);
     const int64_t NW = 3LL * (nx + 1) * S;  // words of a node vector
 
-    float4 *Pn = (float4 *)smem;                // [3][R + 2] operand planes; chunk node l at 1 + l
-    float *Raw = (float *)(Pn + 3 * (R + 2));   // [NR][RW] cp.async buffers
+    const int PR = 4 * ((R + 5) / 4);           // floats per component row (>= R + 2)
+    float *Pn = smem;                           // [3][3][PR] operand planes by component; node l at 1 + l
+    float *Raw = Pn + 9 * PR;                   // [NR][RW] cp.async buffers
     float *Ys = Raw + NR * RW;                  // [RW] output words of the plane
     float2 *Es2 = (float2 *)(Ys + RW);          // [2][NT] element moduli (tid, tid + NT)
     float2 *Z1s = Es2 + 2 * NT;                 // [6][NT] y+1-side contributions (cx, c) per element
@@ -248,7 +252,7 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
     auto commit_plane = [&](int slot, int j) {
         const PlaneW P = plane_w(j);
         cp_async_wait_all();
-        float *Pf = (float *)(Pn + slot * (R + 2) + 1);  // word 4 l + c of chunk node l
+        float *Pf = Pn + slot * 3 * PR + 1;  // component c of chunk node l at Pf[c PR + l]
 #pragma unroll
         for (int q = 0; q < MAXV; ++q) {
             const int f = tid + q * NT;
@@ -331,16 +335,18 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
                         }
                     }
                 }
-                // scatter into the node layout: chunk word cw = 3 l + c -> Pf[4 l + c]; from
-                // the first word's component c0 the next three sit 1 + (c0 == 2), 2 + (c0 != 0)
-                // and 4 floats further (cw0 >= -3, so l >= -1; l <= R; both ends are spare slots)
-                const int l0 = (cw0 + 3) / 3 - 1;
-                const int c0 = cw0 - 3 * l0;
-                float *d0 = Pf + 4 * l0 + c0;
-                d0[0] = val[0];
-                d0[1 + (c0 == 2)] = val[1];
-                d0[2 + (c0 != 0)] = val[2];
-                d0[4] = val[3];
+                // scatter into the component rows: chunk word cw = 3 l + c -> Pf[c PR + l]
+                // (cw0 >= -3, so l >= -1; l <= R; both ends are spare slots)
+                int l = (cw0 + 3) / 3 - 1;
+                int c = cw0 - 3 * l;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    Pf[c * PR + l] = val[k];
+                    if (++c == 3) {
+                        c = 0;
+                        ++l;
+                    }
+                }
             }
         }
     };
@@ -404,11 +410,9 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
                 const int cx = b >> 2, cy = (b >> 1) & 1, cz = b & 1;
-                const float4 *src = Pn + (cx ? s1 : s0) * (R + 2) + 1 + tid + cy * NZ + cz;
-                const float4 wa = src[0], wb = src[NT];
-                v[b][0] = make_float2(wa.x, wb.x);
-                v[b][1] = make_float2(wa.y, wb.y);
-                v[b][2] = make_float2(wa.z, wb.z);
+                const float *src = Pn + (cx ? s1 : s0) * 3 * PR + 1 + tid + cy * NZ + cz;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) v[b][c] = make_float2(src[c * PR], src[c * PR + NT]);
             }
             modal_element2(v, E, km);
         } else {
@@ -441,7 +445,7 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
         __syncthreads();
 
         // ---- nodes of plane i: node l = element l of this thread --------------------------
-        const float4 *Pu = Pn + s0 * (R + 2) + 1;
+        const float *Pu = Pn + s0 * 3 * PR + 1;
         const PlaneW Pi = plane_w(i);
 #pragma unroll
         for (int q = 0; q < EPT; ++q) {
@@ -461,8 +465,7 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
                     }
                 const int flat = F0 - H + l;
                 if (out_plane && flat < S) {
-                    const float4 u4 = Pu[l];
-                    const float uc[3] = {u4.x, u4.y, u4.z};
+                    const float uc[3] = {Pu[l], Pu[PR + l], Pu[2 * PR + l]};
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
                         const float yc = ((om[q] >> c) & 1) ? 0.0f : acc[q][c] + yy[0][c];

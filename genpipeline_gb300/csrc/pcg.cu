@@ -783,6 +783,9 @@ struct ApplyProfile {
     int launches = 0;
 };
 
+// With out == nullptr (and no profiling) the solve is only enqueued: the device-driven paths
+// need no host decision, and the caller reads the scalars later (w.sc of the workspace),
+// together with its own.
 int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x, const float *b,
             const uint8_t *mask, float *u, double rtol, int max_iter, int check_every, void *ws, PcgScalars *out,
             cudaStream_t st, ApplyProfile *prof = nullptr, int fused = 0) {
@@ -792,13 +795,18 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
     int rc = pcg_setup(ctx, nx, ny, nz, glaw, x, b, mask, u, rtol, max_iter, w, st);
     if (rc) return rc;
     PcgScalars h;
-    rc = read_scalars(w.sc, &h, st);
-    if (rc) return rc;
+    memset(&h, 0, sizeof h);
+    const bool async = out == nullptr && !prof;
+    if (!async) {
+        rc = read_scalars(w.sc, &h, st);  // a solve that is done at setup skips the loops
+        if (rc) return rc;
+    }
     if (!prof && !h.done && fused) {
         const FusedItem item{nx, ny, nz, x, mask, u, w};
         if (pcg_fused_batch(ctx, &item, 1, law, st) == GBS_OK) {
             pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, 0);
             GBS_LAUNCH_CHECK("pcg_finalize_kernel");
+            if (async) return GBS_OK;
             rc = read_scalars(w.sc, &h, st);
             if (rc) return rc;
             *out = h;
@@ -812,6 +820,7 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
             GBS_CUDA_TRY(cudaGraphLaunch(exec, st));
             pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 0 : 1);
             GBS_LAUNCH_CHECK("pcg_finalize_kernel");
+            if (async) return GBS_OK;  // the caller counts the loop's launches from the scalars
             rc = read_scalars(w.sc, &h, st);
             if (rc) return rc;
             count_launches(h.trips * launches_per_trip(ctx, nz));
@@ -819,6 +828,10 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
             return GBS_OK;
         }
         // graph construction failed: fall through to host-launched iterations
+    }
+    if (async) {  // the host loop decides from the scalars
+        rc = read_scalars(w.sc, &h, st);
+        if (rc) return rc;
     }
     int chunk = check_every > 0 ? check_every : 16;
     const int max_chunk = check_every > 0 ? check_every : 128;
@@ -941,12 +954,18 @@ __global__ void correct64_kernel(int64_t nd, const float *__restrict__ d, const 
         u[i] = dof_fixed(mask, i) ? 0.0 : fma((double)d[i], s, u[i]);
 }
 
-static int read_outer(const OuterScalars *d, OuterScalars *h, cudaStream_t st) {
-    void *hp = thread_pinned();
+// One host read per defect-correction round: the outer scalars and, when a PCG ran since the
+// last read, its scalars.
+static int read_outer(const OuterScalars *d, OuterScalars *h, const PcgScalars *dp, PcgScalars *hpcg,
+                      cudaStream_t st) {
+    char *hp = (char *)thread_pinned();
     if (!hp) return set_error(GBS_ECUDA, "no pinned staging buffer");
+    static_assert(sizeof(OuterScalars) <= 2048 && sizeof(PcgScalars) <= 2048, "pinned staging layout");
     GBS_CUDA_TRY(cudaMemcpyAsync(hp, d, sizeof(OuterScalars), cudaMemcpyDeviceToHost, st));
+    if (dp) GBS_CUDA_TRY(cudaMemcpyAsync(hp + 2048, dp, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
     GBS_CUDA_TRY(cudaStreamSynchronize(st));
     memcpy(h, hp, sizeof(OuterScalars));
+    if (dp) memcpy(hpcg, hp + 2048, sizeof(PcgScalars));
     return GBS_OK;
 }
 
@@ -962,6 +981,12 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
     double relres = 0.0;
     const int max_outer = o->max_outer > 0 ? o->max_outer : 20;
     const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-4;
+    // Each round: FP64 residual -> one host read (the outer scalars and the previous round's
+    // PCG scalars) -> the decisions -> the inner PCG and the correction, enqueued without a
+    // host read (the graph loop and the persistent kernel are device-driven).
+    const bool async = !o->profile;
+    const PcgScalars *pending = nullptr;
+    const PcgWs pw = pcg_ws(w.pcg, nx, ny, nz);
     for (;;) {
         int rc = ctx->modal_ok ? apply_f64_modal(ctx, nx, ny, nz, law, x, u, w.r64, mask, w.elem, st)
                                : apply_f64(ctx, nx, ny, nz, law, x, u, w.r64, mask, st);
@@ -970,9 +995,19 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
         resid64_kernel<<<vb, 256, 0, st>>>(nd, f, w.r64, mask, w.r64, w.partials, w.os);
         GBS_LAUNCH_CHECK("resid64_kernel");
         OuterScalars h;
-        rc = read_outer(w.os, &h, st);
+        PcgScalars ps;
+        rc = read_outer(w.os, &h, pending, &ps, st);
         if (rc) return rc;
         ++outer;
+        if (pending) {
+            pending = nullptr;
+            total += ps.iter;
+            count_launches(ps.trips * launches_per_trip(ctx, nz));  // graph loop trips (0 for the persistent kernel)
+            // a failed inner solve ends the loop; its correction (zero when it made no step)
+            // is in u and the residual above is the one of the corrected u
+            if (ps.status == GBS_EBREAKDOWN || ps.status == GBS_ENONFINITE || ps.status == GBS_ETIMEOUT)
+                status = ps.status;
+        }
         if (!isfinite(h.rr) || !isfinite(h.ff)) {
             status = GBS_ENONFINITE;
             break;
@@ -983,6 +1018,7 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
             break;
         }
         relres = sqrt(h.rr / h.ff);
+        if (status != GBS_OK) break;
         if (relres <= o->rtol) break;
         if (outer > max_outer || total >= o->max_iter) {
             status = GBS_ENOTCONV;
@@ -993,14 +1029,17 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
         // Inner tolerance: enough to reach rtol from here, but not below what FP32 resolves.
         double itol = o->rtol / relres;
         if (itol < inner) itol = inner;
-        PcgScalars ps;
         rc = pcg_run(ctx, nx, ny, nz, law, x, w.b32, mask, w.d32, itol, o->max_iter - total, o->check_every, w.pcg,
-                     &ps, st, o->profile ? &prof : nullptr, o->fused);
+                     async ? nullptr : &ps, st, o->profile ? &prof : nullptr, o->fused);
         if (rc) return rc;
-        total += ps.iter;
-        if (ps.status == GBS_EBREAKDOWN || ps.status == GBS_ENONFINITE) {
-            status = ps.status;
-            if (ps.iter == 0) break;
+        if (async) {
+            pending = pw.sc;
+        } else {
+            total += ps.iter;
+            if (ps.status == GBS_EBREAKDOWN || ps.status == GBS_ENONFINITE || ps.status == GBS_ETIMEOUT) {
+                status = ps.status;
+                if (ps.iter == 0) break;
+            }
         }
         correct64_kernel<<<vb, 256, 0, st>>>(nd, w.d32, w.os, mask, u);
         GBS_LAUNCH_CHECK("correct64_kernel");
