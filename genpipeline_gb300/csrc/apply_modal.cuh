@@ -42,14 +42,14 @@ struct ModalGeom {
 // cp.async buffers (one per staged vector: p for the
 // plain apply; r, w, s, 1/diag, p, x for the PCG modes) and the output words of a plane,
 // each 4 * ceil((3R + 3) / 4) floats, two planes of element moduli, the y-direction slots
-// (6 floats per element) and the warp-boundary contributions (12 floats per warp and lane).
+// (3 floats per element) and the warp-boundary contributions (6 floats per warp and lane).
 template <int NT, int EPT>
 inline size_t modal_smem_bytes(int nz, bool cg) {
     const int NE = NT * EPT, H = nz + 2, R = NE + H;
     const size_t RW = 4 * (size_t)((3 * R + 6) / 4);
     const size_t PR = 4 * (size_t)((R + 5) / 4);
     return 9 * PR * sizeof(float) + ((cg ? 6 : 1) + 1) * RW * sizeof(float) +
-           (2 + 6) * (size_t)NT * sizeof(float2) + (size_t)(NT / 32) * 12 * sizeof(float2);
+           (2 + 3) * (size_t)NT * sizeof(float2) + (size_t)(NT / 32) * 6 * sizeof(float2);
 }
 
 // cp.async (sm_80+): 16-byte global -> shared copies through L2 that use no registers;
@@ -73,6 +73,9 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b
 // Two elements at once: corners v[b][c] (b = cx*4 + cy*2 + cz) -> E (Ke p_e)_b,c for each
 // lane. The operations and their order per lane are those of the scalar form: forward
 // butterflies, r = Km q (each row summed in column order), r *= E, inverse butterflies.
+// With XONLY the inverse stops after its x stage: v[b] (b < 4) is then the (y, z)-modal cx = 0
+// half and v[4 + b] the cx = 1 half, to be summed per node plane before yz_inverse2.
+template <bool XONLY>
 __device__ __forceinline__ void modal_element2(float2 (&v)[8][3], float2 E, const ModalK &km) {
     // forward Walsh-Hadamard per component: (u0, u1) -> (u0 + u1, u1 - u0)
 #pragma unroll
@@ -115,10 +118,10 @@ __device__ __forceinline__ void modal_element2(float2 (&v)[8][3], float2 E, cons
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) v[0][c] = make_float2(0.0f, 0.0f);
-    // inverse: (r0, r1) -> (r0 - r1, r0 + r1) along each axis
+    // inverse: (r0, r1) -> (r0 - r1, r0 + r1) along each axis (x first; the stages commute)
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const int bit = 1 << d;
+    for (int dd = 0; dd < (XONLY ? 1 : 3); ++dd) {
+        const int bit = 4 >> dd;
 #pragma unroll
         for (int b = 0; b < 8; ++b) {
             if (b & bit) continue;
@@ -127,6 +130,25 @@ __device__ __forceinline__ void modal_element2(float2 (&v)[8][3], float2 E, cons
                 const float2 r0 = v[b][c], r1 = v[b | bit][c];
                 v[b][c] = sub2(r0, r1);
                 v[b | bit][c] = add2(r0, r1);
+            }
+        }
+    }
+}
+
+// The (y, z) stages of the inverse transform on one node plane's four corners
+// (b = cy * 2 + cz): (r0, r1) -> (r0 - r1, r0 + r1) along z, then along y.
+__device__ __forceinline__ void yz_inverse2(float2 (&h)[4][3]) {
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+        const int bit = 1 << d;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            if (b & bit) continue;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float2 r0 = h[b][c], r1 = h[b | bit][c];
+                h[b][c] = sub2(r0, r1);
+                h[b | bit][c] = add2(r0, r1);
             }
         }
     }
@@ -190,8 +212,8 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
     float *Raw = Pn + 9 * PR;                   // [NR][RW] cp.async buffers
     float *Ys = Raw + NR * RW;                  // [RW] output words of the plane
     float2 *Es2 = (float2 *)(Ys + RW);          // [2][NT] element moduli (tid, tid + NT)
-    float2 *Z1s = Es2 + 2 * NT;                 // [6][NT] y+1-side contributions (cx, c) per element
-    float2 *Bd = Z1s + 6 * NT;                  // [NT/32][12] z+1-side contributions of lane 31
+    float2 *Z1s = Es2 + 2 * NT;                 // [3][NT] y+1-side contributions (c) per element
+    float2 *Bd = Z1s + 3 * NT;                  // [NT/32][6] z+1-side contributions (cy, c) of lane 31
     const float *Z1f = (const float *)Z1s;
     const float *Bdf = (const float *)Bd;
 
@@ -365,11 +387,11 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
         Es2[slot * NT + tid] =
             make_float2(eok[0] ? modulus(law, ex[0]) : 0.0f, eok[1] ? modulus(law, ex[1]) : 0.0f);
     };
-    // z+1-side contribution (cx, cy, c) of element e - 1 where e sits in lane 0
-    auto boundary = [&](int e, int cx, int cy, int c) -> float {
+    // z+1-side contribution (cy, c) of element e - 1 where e sits in lane 0
+    auto boundary = [&](int e, int cy, int c) -> float {
         const int pe = e - 1;
         const int pt = pe >= NT ? pe - NT : pe;
-        return Bdf[2 * ((pt >> 5) * 12 + (cx * 2 + cy) * 3 + c) + (pe >= NT ? 1 : 0)];
+        return Bdf[2 * ((pt >> 5) * 6 + cy * 3 + c) + (pe >= NT ? 1 : 0)];
     };
 
     // ---- prologue: node planes xs-1, xs and element plane xs-1 (the raw buffers hold one
@@ -382,9 +404,13 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
     commit_plane(1, xs);
     __syncthreads();
 
-    float acc[EPT][3];
+    // x-direction carry: the cx = 1 half of element plane i - 1 in the (y, z) modal basis,
+    // which belongs to node plane i together with the cx = 0 half of element plane i
+    float2 g1[4][3];
 #pragma unroll
-    for (int q = 0; q < EPT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = 0.0f;
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) g1[b][c] = make_float2(0.0f, 0.0f);
 
     for (int i = xs - 1; i < xe; ++i) {  // modal_geom makes every segment non-empty
         const int k = i - (xs - 1);
@@ -404,9 +430,12 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
         }
 
         // ---- element plane i: elements tid and tid + NT as the two lanes of a float2 ----
-        float2 v[8][3];
+        // h: the contributions of element planes i - 1 (carried) and i to node plane i, summed
+        // in the (y, z) modal basis, then transformed back
+        float2 h[4][3];
         if (i >= 0 && i < nx) {
             const float2 E = Es2[es * NT + tid];
+            float2 v[8][3];
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
                 const int cx = b >> 2, cy = (b >> 1) & 1, cz = b & 1;
@@ -414,31 +443,38 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
 #pragma unroll
                 for (int c = 0; c < 3; ++c) v[b][c] = make_float2(src[c * PR], src[c * PR + NT]);
             }
-            modal_element2(v, E, km);
+            modal_element2<true>(v, E, km);
+#pragma unroll
+            for (int b = 0; b < 4; ++b)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    h[b][c] = add2(v[b][c], g1[b][c]);
+                    g1[b][c] = v[4 + b][c];
+                }
         } else {
 #pragma unroll
-            for (int b = 0; b < 8; ++b)
+            for (int b = 0; b < 4; ++b)
 #pragma unroll
-                for (int c = 0; c < 3; ++c) v[b][c] = make_float2(0.0f, 0.0f);
+                for (int c = 0; c < 3; ++c) {
+                    h[b][c] = g1[b][c];
+                    g1[b][c] = make_float2(0.0f, 0.0f);
+                }
         }
+        yz_inverse2(h);  // h[cy * 2 + cz]: contribution to corner (cy, cz) of node plane i
         // z: the cz = 1 corners of element e - 1 (lane - 1) join the cz = 0 corners of e
-        float2 z0[2][3];
+        float2 z0[3];
 #pragma unroll
-        for (int cx = 0; cx < 2; ++cx)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                float2 a1 = shfl_up2(v[cx * 4 + 1][c]), b1 = shfl_up2(v[cx * 4 + 3][c]);
-                if (lane == 0) a1 = b1 = make_float2(0.0f, 0.0f);
-                z0[cx][c] = add2(v[cx * 4 + 0][c], a1);
-                Z1s[(cx * 3 + c) * NT + tid] = add2(v[cx * 4 + 2][c], b1);
-            }
+        for (int c = 0; c < 3; ++c) {
+            float2 a1 = shfl_up2(h[1][c]), b1 = shfl_up2(h[3][c]);
+            if (lane == 0) a1 = b1 = make_float2(0.0f, 0.0f);
+            z0[c] = add2(h[0][c], a1);
+            Z1s[c * NT + tid] = add2(h[2][c], b1);
+        }
         if (lane == 31) {
 #pragma unroll
-            for (int cx = 0; cx < 2; ++cx)
+            for (int cy = 0; cy < 2; ++cy)
 #pragma unroll
-                for (int cy = 0; cy < 2; ++cy)
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) Bd[warp * 12 + (cx * 2 + cy) * 3 + c] = v[cx * 4 + cy * 2 + 1][c];
+                for (int c = 0; c < 3; ++c) Bd[warp * 6 + cy * 3 + c] = h[cy * 2 + 1][c];
         }
         if (more_nodes) commit_plane(s2, i + 2);
         if (more_elems) commit_eplane(es ^ 1);
@@ -450,31 +486,20 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
 #pragma unroll
         for (int q = 0; q < EPT; ++q) {
             const int l = tid + q * NT;
-            if (l >= H) {
+            const int flat = F0 - H + l;
+            if (l >= H && out_plane && flat < S) {
                 const int m = l - NZ;  // element whose y+1 corners touch node l (m >= 1)
                 const int mi = m >= NT ? 2 * (m - NT) + 1 : 2 * m;
-                float yy[2][3];
+                const float uc[3] = {Pu[l], Pu[PR + l], Pu[2 * PR + l]};
 #pragma unroll
-                for (int cx = 0; cx < 2; ++cx)
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        float s = (q ? z0[cx][c].y : z0[cx][c].x) + Z1f[(cx * 3 + c) * 2 * NT + mi];
-                        if (lane == 0) s += boundary(l, cx, 0, c);
-                        if ((m & 31) == 0) s += boundary(m, cx, 1, c);
-                        yy[cx][c] = s;
-                    }
-                const int flat = F0 - H + l;
-                if (out_plane && flat < S) {
-                    const float uc[3] = {Pu[l], Pu[PR + l], Pu[2 * PR + l]};
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        const float yc = ((om[q] >> c) & 1) ? 0.0f : acc[q][c] + yy[0][c];
-                        if (CG) g_wu = fmaf(uc[c], yc, g_wu);
-                        Ys[Pi.pad + 3 * l + c] = yc;
-                    }
+                for (int c = 0; c < 3; ++c) {
+                    float s = (q ? z0[c].y : z0[c].x) + Z1f[c * 2 * NT + mi];
+                    if (lane == 0) s += boundary(l, 0, c);
+                    if ((m & 31) == 0) s += boundary(m, 1, c);
+                    const float yc = ((om[q] >> c) & 1) ? 0.0f : s;
+                    if (CG) g_wu = fmaf(uc[c], yc, g_wu);
+                    Ys[Pi.pad + 3 * l + c] = yc;
                 }
-#pragma unroll
-                for (int c = 0; c < 3; ++c) acc[q][c] = yy[1][c];
             }
         }
         __syncthreads();
