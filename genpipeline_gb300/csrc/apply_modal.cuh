@@ -180,13 +180,15 @@ __device__ __forceinline__ float ld_vec(const float *p) {
 // One sliding-window pass of a CTA over its (flat tile, x segment): y = D K D p on the owned
 // nodes (PLAIN), or one PCG iteration with y = w_{i+1} (CG modes). sums[] receives this
 // thread's FP32 shares of r.u, w.u and r.r (CG modes). Every node vector must be 16-byte
-// aligned.
-template <int NT, int EPT, int MAXV, int MODE>
-__device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__restrict__ x,
+// aligned. pre(alpha, beta) runs once the first plane's copies are in flight (the step's
+// scalars can be formed meanwhile); when it returns false the pass stops there (returns
+// false).
+template <int NT, int EPT, int MAXV, int MODE, typename Pre>
+__device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__restrict__ x,
                                            const float *__restrict__ p, float *__restrict__ y,
                                            const uint8_t *__restrict__ mask, const Law<float> &law,
                                            const ModalK &km, const CgPass &cp, float *smem, int tile, int seg,
-                                           float (&sums)[3]) {
+                                           float (&sums)[3], Pre &&pre) {
     constexpr int NE = NT * EPT;
     constexpr bool CG = MODE == MODE_CG || MODE == MODE_CG_FUSED;
     constexpr int NR = CG ? 6 : 1;  // staged vectors
@@ -217,8 +219,9 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
     const float *Z1f = (const float *)Z1s;
     const float *Bdf = (const float *)Bd;
 
-    const float alpha = cp.alpha, beta = cp.beta;
+    float alpha = cp.alpha, beta = cp.beta;
     float g_ru = 0.0f, g_wu = 0.0f, g_rr = 0.0f;  // FP32 per-thread partials
+    sums[0] = sums[1] = sums[2] = 0.0f;
 
     auto src_of = [&](int a) -> const float * {
         if (!CG) return p;
@@ -398,6 +401,10 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
     // plane: the second plane's copies go out after the first plane is combined) ----------
     issue_plane(xs - 1);
     issue_eplane(xs - 1);
+    if (!pre(alpha, beta)) {
+        cp_async_wait_all();  // no copy may land after the CTA has left
+        return false;
+    }
     commit_plane(0, xs - 1);
     issue_plane(xs);
     commit_eplane(0);
@@ -529,6 +536,7 @@ __device__ __forceinline__ void modal_pass(const ModalGeom &G, const float *__re
     sums[0] = g_ru;
     sums[1] = g_wu;
     sums[2] = g_rr;
+    return true;
 }
 
 // The scalar step at the end of PCG iteration i, from gamma = r_{i+1}.u_{i+1},
@@ -564,69 +572,93 @@ __device__ __forceinline__ void cg_scalar_step(double gamma, double delta, doubl
     }
 }
 
+// Folds the block partial sums (r.u, w.u, r.r; double-float, slot layout [k][nblk]) of the
+// pass that started from state s into s: the scalar step of that iteration. Every block of the
+// next launch does it, in the same order (deterministic), instead of a last block of the pass.
+// All threads of the block take part; the sums stay off the FP64 pipe.
+template <int NT>
+__device__ __forceinline__ void cg_fold(CgState &s, const PcgScalars *sc, const float2 *partials, int nblk,
+                                        float2 *sred) {
+    __shared__ CgState sh;
+    df32 tot[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+    for (int b = threadIdx.x; b < nblk; b += NT)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float2 v = __ldcg(&partials[k * nblk + b]);
+            tot[k] = df_add(tot[k], df32{v.x, v.y});
+        }
+    block_sum_df<3>(tot, sred);
+    if (threadIdx.x == 0) {
+        int it = s.iter, done = 0, status = s.status;
+        double g = s.gamma, a = s.alpha, b = s.beta;
+        const double t0 = df_value(tot[0]), t1 = df_value(tot[1]), t2 = df_value(tot[2]);
+        cg_scalar_step(t0, t1, t2, sc->tol, sc->bnorm, sc->max_iter, it, done, status, g, a, b);
+        s.iter = it;
+        s.done = done;
+        s.status = status;
+        s.gamma = g;
+        s.alpha = a;
+        s.beta = b;
+        s.rr = t2;
+        s.pap = t1;
+        s.pending = 0;
+        sh = s;
+    }
+    __syncthreads();
+    s = sh;
+}
+
+// par: launch parity (k & 1 for the k-th launch of a solve; the graph loop and the host loops
+// know it statically). MODE_CG reads state slot par ^ 1 and partial slot par ^ 1, writes
+// state slot par (block 0) and partial slot par.
 template <int NT, int EPT, int MAXV, int MODE>
 __global__ void __launch_bounds__(NT, 2)
     apply_modal_kernel(ModalGeom G, const float *__restrict__ x, const float *__restrict__ p, float *__restrict__ y,
-                       const uint8_t *__restrict__ mask, Law<float> law, const ModalK km, CgArgs ca) {
+                       const uint8_t *__restrict__ mask, Law<float> law, const ModalK km, CgArgs ca, int par) {
     extern __shared__ float4 smem4[];
-    __shared__ double sred[3 * 32];
+    __shared__ float2 sred[3 * 32];
     const int tid = threadIdx.x;
+    const int nblk = gridDim.x * gridDim.y;
+    const int bid = blockIdx.x + gridDim.x * blockIdx.y;
     CgPass cp{0.0f, 0.0f, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-    int it = 0;
     if (MODE == MODE_CG) {
-        const PcgScalars *sc = ca.sc;
-        const int done = sc->done;
-        it = sc->iter;
-        const double a = sc->alpha[0], b = sc->beta;
-        if (done) return;
-        // parity selects (a dynamic index into the parameter arrays would copy them to the stack)
-        const bool odd = it & 1;
+        // Launch k runs iteration k while the solve lasts, so the vector parity is the launch
+        // parity: the first plane's copies go out before the state is known.
+        const bool odd = par;  // parity selects (a dynamic index into the parameter arrays would copy them to the stack)
         float *r_c = odd ? ca.r[1] : ca.r[0], *r_n = odd ? ca.r[0] : ca.r[1];
         float *w_c = odd ? ca.w[1] : ca.w[0], *w_n = odd ? ca.w[0] : ca.w[1];
         float *s_c = odd ? ca.s[1] : ca.s[0], *s_n = odd ? ca.s[0] : ca.s[1];
-        cp = CgPass{(float)a, (float)b, r_c, w_c, s_n, ca.dinv, r_n, s_c, ca.p, ca.xu};
+        cp = CgPass{0.0f, 0.0f, r_c, w_c, s_n, ca.dinv, r_n, s_c, ca.p, ca.xu};
         y = w_n;
     }
-    float sums[3];
-    modal_pass<NT, EPT, MAXV, MODE>(G, x, p, y, mask, law, km, cp, (float *)smem4, blockIdx.x, blockIdx.y, sums);
-    if (MODE == MODE_CG) {
-        const int nblk = gridDim.x * gridDim.y;
-        const int bid = blockIdx.x + gridDim.x * blockIdx.y;
-        double bs[3] = {(double)sums[0], (double)sums[1], (double)sums[2]};
-        block_sum_n<3>(bs, sred);
-        __shared__ bool last;
-        if (tid == 0) {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) ca.partials[k * nblk + bid] = bs[k];
-            __threadfence();
-            last = (atomicAdd(&ca.sc->counter, 1u) == (unsigned)(nblk - 1));
-        }
-        __syncthreads();
-        if (last) {
-            __threadfence();
-            double tot[3] = {0.0, 0.0, 0.0};
-            for (int b = tid; b < nblk; b += NT)
-#pragma unroll
-                for (int k = 0; k < 3; ++k) tot[k] += __ldcg(&ca.partials[k * nblk + b]);
-            block_sum_n<3>(tot, sred);
-            if (tid == 0) {
-                PcgScalars *sc = ca.sc;
-                sc->counter = 0;
-                if (!sc->freeze) {
-                    int done = 0, status = GBS_OK;
-                    double gamma_i = sc->rz, alpha = sc->alpha[0], beta = sc->beta;
-                    cg_scalar_step(tot[0], tot[1], tot[2], sc->tol, sc->bnorm, sc->max_iter, it, done, status, gamma_i,
-                                   alpha, beta);
-                    sc->iter = it;
-                    sc->rr = tot[2];
-                    sc->pap = tot[1];
-                    sc->rz = gamma_i;
-                    sc->alpha[0] = alpha;
-                    sc->beta = beta;
-                    sc->status = status;
-                    sc->done = done;
-                }
+    auto pre = [&](float &alpha, float &beta) -> bool {
+        if (MODE != MODE_CG) return true;
+        const PcgScalars *sc = ca.sc;
+        CgState s = sc->st[par ^ 1];
+        if (!sc->freeze) {
+            if (s.pending && !s.done)
+                cg_fold<NT>(s, sc, (const float2 *)ca.partials + (par ^ 1) * 3 * nblk, nblk, sred);
+            if (bid == 0 && tid == 0) {
+                CgState o = s;
+                o.pending = s.done ? 0 : 1;
+                ca.sc->st[par] = o;
             }
+        }
+        alpha = (float)s.alpha;
+        beta = (float)s.beta;
+        return !s.done;
+    };
+    float sums[3];
+    if (!modal_pass<NT, EPT, MAXV, MODE>(G, x, p, y, mask, law, km, cp, (float *)smem4, blockIdx.x, blockIdx.y, sums,
+                                         pre))
+        return;
+    if (MODE == MODE_CG) {
+        df32 bs[3] = {{sums[0], 0.0f}, {sums[1], 0.0f}, {sums[2], 0.0f}};
+        block_sum_df<3>(bs, sred);
+        if (tid == 0) {
+            float2 *part = (float2 *)ca.partials + par * 3 * nblk;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) part[k * nblk + bid] = make_float2(bs[k].hi, bs[k].lo);
         }
     }
 }
@@ -703,20 +735,30 @@ inline int modal_prepare(const gbsimp_ctx *ctx, int nz) {
     return modal_short(nz) ? modal_prepare_one<MODE, 2>(ctx, nz) : modal_prepare_one<MODE, 3>(ctx, nz);
 }
 
+// CTAs of the modal kernel's launch for a grid (the partial sums of one MODE_CG pass).
+template <int MODE>
+inline int modal_blocks(const gbsimp_ctx *ctx, int nx, int ny, int nz) {
+    const int per_sm = modal_prepare<MODE>(ctx, nz);
+    if (per_sm < 0) return per_sm;
+    const dim3 g = modal_grid(modal_geom(nx, ny, nz, ctx->num_sms, per_sm));
+    return (int)(g.x * g.y);
+}
+
 // Launches the modal kernel (MODE_PLAIN: y = D K D p; MODE_CG: one PCG iteration).
 template <int MODE>
 inline int launch_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
-                        const float *p, float *y, const uint8_t *mask, const CgArgs &ca, cudaStream_t st) {
+                        const float *p, float *y, const uint8_t *mask, const CgArgs &ca, cudaStream_t st,
+                        int par = 0) {
     const int per_sm = modal_prepare<MODE>(ctx, nz);
     if (per_sm < 0) return -per_sm;
     const size_t smem = modal_smem_bytes<kModalNT, kModalEPT>(nz, MODE != MODE_PLAIN);
     const ModalGeom g = modal_geom(nx, ny, nz, ctx->num_sms, per_sm);
     if (modal_short(nz))
         apply_modal_kernel<kModalNT, kModalEPT, 2, MODE>
-            <<<modal_grid(g), kModalNT, smem, st>>>(g, x, p, y, mask, law, ctx->km, ca);
+            <<<modal_grid(g), kModalNT, smem, st>>>(g, x, p, y, mask, law, ctx->km, ca, par);
     else
         apply_modal_kernel<kModalNT, kModalEPT, 3, MODE>
-            <<<modal_grid(g), kModalNT, smem, st>>>(g, x, p, y, mask, law, ctx->km, ca);
+            <<<modal_grid(g), kModalNT, smem, st>>>(g, x, p, y, mask, law, ctx->km, ca, par);
     GBS_LAUNCH_CHECK("apply_modal_kernel");
     return GBS_OK;
 }

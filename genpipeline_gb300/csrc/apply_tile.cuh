@@ -26,6 +26,14 @@ namespace gbs {
 // (L1 is not coherent across SMs within one launch).
 enum { MODE_PLAIN = 0, MODE_PCG = 1, MODE_CG = 3, MODE_CG_FUSED = 4 };
 
+// State of the one-kernel PCG at the start of an iteration. Launch k writes slot k & 1 and
+// reads slot (k & 1) ^ 1; `pending` marks a state whose pass has written block partial sums
+// (slot k & 1 of the partials) that the next launch folds in before its own pass.
+struct CgState {
+    double alpha, beta, gamma, rr, pap;
+    int iter, done, status, pending;
+};
+
 // Device-resident state of one Jacobi-PCG solve (FP32 vectors, FP64 scalars).
 struct PcgScalars {
     double rz;        // r_k . z_k
@@ -44,6 +52,7 @@ struct PcgScalars {
     int trips;        // WHILE-loop trips run by the device-driven loop
     int max_trips;    // hard cap on those trips (the loop always ends)
     int freeze;       // 1 = kernels leave the scalars as they are (timing of one pass)
+    CgState st[2];    // one-kernel PCG: the state by launch parity
 };
 
 struct PcgArgs {
@@ -65,7 +74,7 @@ struct CgArgs {
     float *p;           // search direction
     float *xu;          // iterate
     const float *dinv;  // M = 1/diag(K) on free DOFs, 0 on fixed DOFs
-    double *partials;   // three doubles per block
+    double *partials;   // per block three double-float sums (float2 hi, lo) in two parity slots
     PcgScalars *sc;     // alpha[0] = alpha_i, beta = beta_i, rz = gamma_i = r_i.u_i
 };
 

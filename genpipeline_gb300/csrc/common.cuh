@@ -146,6 +146,54 @@ __device__ __forceinline__ void block_sum_n(double (&v)[K], double *scratch) {
     }
 }
 
+// Double-float sums: a value hi + lo held as two FP32 numbers, added with the exact two-sum
+// error term (Knuth), about 48 significant bits. Used for the block and grid sums of the
+// PCG iteration, where FP64 adds would run on the narrow FP64 pipe. The add is commutative,
+// so butterfly reductions leave every lane with the same value.
+struct df32 {
+    float hi, lo;
+};
+__device__ __forceinline__ df32 df_add(df32 a, df32 b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    const float hi = __fadd_rn(s, e);
+    const float lo = __fsub_rn(e, __fsub_rn(hi, s));
+    return df32{hi, lo};
+}
+__device__ __forceinline__ double df_value(df32 a) { return (double)a.hi + (double)a.lo; }
+
+// K block sums in double-float with one pair of barriers; valid in thread 0. scratch: 32 K
+// float2.
+template <int K>
+__device__ __forceinline__ void block_sum_df(df32 (&v)[K], float2 *scratch) {
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int lane = tid & 31, warp = tid >> 5;
+    const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v[k] = df_add(v[k], df32{__shfl_xor_sync(0xffffffffu, v[k].hi, o), __shfl_xor_sync(0xffffffffu, v[k].lo, o)});
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; ++k) scratch[32 * k + warp] = make_float2(v[k].hi, v[k].lo);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        df32 r{0.0f, 0.0f};
+        if (warp == 0) {
+            if (lane < nw) r = df32{scratch[32 * k + lane].x, scratch[32 * k + lane].y};
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                r = df_add(r, df32{__shfl_xor_sync(0xffffffffu, r.hi, o), __shfl_xor_sync(0xffffffffu, r.lo, o)});
+        }
+        v[k] = r;
+    }
+}
+
 constexpr int kModalNnz = 45;
 
 // Modal form of the isotropic cube element (see apply_modal.cuh). Sparsity pattern of Km in (mode*3 + component) indices (derived from the quadrature

@@ -241,7 +241,17 @@ __global__ void cg_init_kernel(int64_t nd, const float *__restrict__ b, float *q
 // beta_0 = 0.
 __global__ void cg_start_kernel(int64_t nd, const float *__restrict__ w, const float *__restrict__ u,
                                 double *partials, PcgScalars *sc) {
-    if (sc->done) return;
+    if (sc->done) {  // the first launch reads state slot 1
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            CgState s = {};
+            s.done = 1;
+            s.status = sc->status;
+            s.rr = sc->rr;
+            s.gamma = sc->rz;
+            sc->st[1] = s;
+        }
+        return;
+    }
     float wu = 0.0f;
     for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x)
         wu = fmaf(w[d], u[d], wu);
@@ -258,6 +268,34 @@ __global__ void cg_start_kernel(int64_t nd, const float *__restrict__ w, const f
             sc->alpha[0] = sc->rz / tot[0];
             sc->beta = 0.0;
         }
+        CgState s = {};
+        s.alpha = sc->alpha[0];
+        s.gamma = sc->rz;
+        s.rr = sc->rr;
+        s.pap = tot[0];
+        s.done = sc->done;
+        s.status = sc->status;
+        sc->st[1] = s;
+    }
+}
+
+// After a run of one-kernel PCG launches (the last one of parity `last`): folds that launch's
+// pending partial sums and publishes the state in the host-visible fields. A status already
+// set on the host-visible side (the loop's trip cap) is kept.
+__global__ void cg_fold_kernel(int nblk, int last, double *partials, PcgScalars *sc) {
+    __shared__ float2 sred[3 * 32];
+    CgState s = sc->st[last];
+    if (s.pending && !s.done) cg_fold<256>(s, sc, (const float2 *)partials + last * 3 * nblk, nblk, sred);
+    if (threadIdx.x == 0) {
+        sc->st[last] = s;
+        sc->iter = s.iter;
+        sc->rz = s.gamma;
+        sc->rr = s.rr;
+        sc->pap = s.pap;
+        sc->alpha[0] = s.alpha;
+        sc->beta = s.beta;
+        if (sc->status == GBS_OK) sc->status = s.status;
+        sc->done = sc->done || s.done;
     }
 }
 
@@ -318,9 +356,10 @@ static int read_scalars(const PcgScalars *d, PcgScalars *h, cudaStream_t st) {
 
 // Launches one iteration: the single-reduction kernel (modal element) or K1 + K2.
 static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
-                         const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st, cudaEvent_t after_k1) {
+                         const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st, cudaEvent_t after_k1,
+                         int par) {
     if (use_modal(ctx, nz)) {
-        int rc = launch_modal<MODE_CG>(ctx, nx, ny, nz, law, x, nullptr, nullptr, mask, cg_args(w, u), st);
+        int rc = launch_modal<MODE_CG>(ctx, nx, ny, nz, law, x, nullptr, nullptr, mask, cg_args(w, u), st, par);
         if (rc) return rc;
         if (after_k1) GBS_CUDA_TRY(cudaEventRecord(after_k1, st));
         return GBS_OK;
@@ -465,7 +504,7 @@ __global__ void __launch_bounds__(NT, 2)
         const CgPass cp{(float)alpha, (float)beta, ca.r[c], ca.w[c], ca.s[nc], ca.dinv, ca.r[nc], ca.s[c], ca.p, ca.xu};
         float sums[3];
         modal_pass<NT, EPT, MAXV, MODE_CG_FUSED>(G, D.x, nullptr, ca.w[nc], D.mask, law, km, cp, (float *)smem4, tile, seg,
-                                                 sums);
+                                                 sums, [](float &, float &) { return true; });
         __threadfence();
         target += nblk;
         double tot[3];
@@ -612,7 +651,7 @@ static inline int launches_per_trip(const gbsimp_ctx *ctx, int nz) {
 __global__ void pcg_loop_cond_kernel(cudaGraphConditionalHandle h, PcgScalars *sc) {
     const int trips = sc->trips + 1;
     sc->trips = trips;
-    bool stop = sc->done != 0;
+    bool stop = sc->done != 0 || sc->st[1].done != 0;  // (a trip ends with a launch of parity 1)
     if (!stop && trips >= sc->max_trips) {
         sc->done = 1;
         sc->status = GBS_ETIMEOUT;
@@ -647,7 +686,18 @@ struct LoopKey {
 };
 
 static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
-                         const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st, cudaEvent_t after_k1);
+                         const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st, cudaEvent_t after_k1,
+                         int par);
+
+// Publishes the state after one-kernel PCG launches (last launch of parity `last`).
+static int cg_publish(const gbsimp_ctx *ctx, int nx, int ny, int nz, const PcgWs &w, int last, cudaStream_t st) {
+    if (!use_modal(ctx, nz)) return GBS_OK;
+    const int nblk = modal_blocks<MODE_CG>(ctx, nx, ny, nz);
+    if (nblk < 0) return -nblk;
+    cg_fold_kernel<<<1, 256, 0, st>>>(nblk, last, w.partials, w.sc);
+    GBS_LAUNCH_CHECK("cg_fold_kernel");
+    return GBS_OK;
+}
 
 // Builds (or finds) the instantiated loop graph for this problem and buffer set.
 static int loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
@@ -719,7 +769,7 @@ static int loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<f
         }
         set_capturing(true);
         for (int i = 0; i < kLoopUnroll && rc == GBS_OK; ++i)
-            rc = pcg_iteration(ctx, nx, ny, nz, law, x, mask, u, w, gc->cap, nullptr);
+            rc = pcg_iteration(ctx, nx, ny, nz, law, x, mask, u, w, gc->cap, nullptr, i & 1);
         if (rc == GBS_OK) {
             pcg_loop_cond_kernel<<<1, 1, 0, gc->cap>>>(h, w.sc);
             e = cudaGetLastError();
@@ -818,6 +868,8 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
         cudaGraphExec_t exec = nullptr;
         if (loop_graph(ctx, nx, ny, nz, law, x, mask, u, w, &exec) == GBS_OK) {
             GBS_CUDA_TRY(cudaGraphLaunch(exec, st));
+            rc = cg_publish(ctx, nx, ny, nz, w, 1, st);
+            if (rc) return rc;
             pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 0 : 1);
             GBS_LAUNCH_CHECK("pcg_finalize_kernel");
             if (async) return GBS_OK;  // the caller counts the loop's launches from the scalars
@@ -846,10 +898,13 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
         const int it0 = h.iter;
         for (int i = 0; i < n; ++i) {
             if (prof) GBS_CUDA_TRY(cudaEventRecord(ev[2 * i], st));
-            rc = pcg_iteration(ctx, nx, ny, nz, law, x, mask, u, w, st, prof ? ev[2 * i + 1] : nullptr);
+            rc = pcg_iteration(ctx, nx, ny, nz, law, x, mask, u, w, st, prof ? ev[2 * i + 1] : nullptr,
+                               (launched + i) & 1);
             if (rc) return rc;
         }
         launched += n;
+        rc = cg_publish(ctx, nx, ny, nz, w, (launched - 1) & 1, st);
+        if (rc) return rc;
         rc = read_scalars(w.sc, &h, st);
         if (rc) return rc;
         if (prof) {
@@ -1246,8 +1301,10 @@ extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, co
     fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 1.0f, w.r);
     fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.p1);
     fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, xu);
-    if (modal) {
+    if (modal) {  // launches alternate the buffer parity: give both parities the same state
+        fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 1.0f, w.r1);
         fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.ap);
+        fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.s0);
         fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.s1);
         fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.p0);
         freeze_scalars_kernel<<<1, 1, 0, st>>>(w.sc);
@@ -1266,7 +1323,8 @@ extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, co
     PcgArgs pa{w.r, w.dinv, w.p0, w.p1, xu, w.partials, w.sc};
     for (int i = 0; i < reps && rc == GBS_OK; ++i) {
         if (modal) {
-            rc = launch_modal<MODE_CG>(ctx, nx, ny, nz, law, x, nullptr, nullptr, node_mask, cg_args(w, xu), gc->cap);
+            rc = launch_modal<MODE_CG>(ctx, nx, ny, nz, law, x, nullptr, nullptr, node_mask, cg_args(w, xu), gc->cap,
+                                       i & 1);
         } else {
             TileArgs<float> A{nx, ny, nz, x, nullptr, w.ap, node_mask};
             const dim3 g = tile_grid<TileF>(nx, ny, nz), b = tile_block<TileF>();
@@ -1515,6 +1573,8 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
         int rc = loop_graph(ctx, it.nx, it.ny, it.nz, law, it.x, it.node_mask, w.d32, pw, &exec);
         if (rc) return rc;
         GBS_CUDA_TRY(cudaGraphLaunch(exec, st));
+        rc = cg_publish(ctx, it.nx, it.ny, it.nz, pw, 1, st);
+        if (rc) return rc;
     }
     // finalize, read every item's PCG scalars (one sync), correct u
     const size_t ps = sizeof(PcgScalars);
