@@ -572,10 +572,39 @@ __device__ __forceinline__ void cg_scalar_step(double gamma, double delta, doubl
     }
 }
 
+// cg_scalar_step in double-float, for the one-kernel PCG: the same recurrence and stop
+// tests, with r.r compared against rr_stop = (tol ||D b||)^2 (no square root; r.r = 0 also
+// stops, for a threshold below the FP32 range).
+__device__ __forceinline__ void cg_scalar_step_df(df32 gamma, df32 delta, df32 rho, float rr_stop, int max_iter,
+                                                  int &it, int &done, int &status, df32 &gamma_i, df32 &alpha,
+                                                  df32 &beta) {
+    it += 1;
+    if (!isfinite(gamma.hi) || !isfinite(delta.hi) || !isfinite(rho.hi)) {
+        done = 1;
+        status = GBS_ENONFINITE;
+    } else if (rho.hi < rr_stop || rho.hi == 0.0f) {
+        done = 1;
+    } else if (it >= max_iter) {
+        done = 1;
+        status = GBS_ENOTCONV;
+    } else {
+        const df32 b1 = df_div(gamma, gamma_i);
+        const df32 den = df_add(delta, df_neg(df_mul(b1, df_div(gamma, alpha))));
+        if (!(den.hi > 0.0f)) {
+            done = 1;
+            status = GBS_EBREAKDOWN;
+        } else {
+            alpha = df_div(gamma, den);
+            beta = b1;
+            gamma_i = gamma;
+        }
+    }
+}
+
 // Folds the block partial sums (r.u, w.u, r.r; double-float, slot layout [k][nblk]) of the
 // pass that started from state s into s: the scalar step of that iteration. Every block of the
 // next launch does it, in the same order (deterministic), instead of a last block of the pass.
-// All threads of the block take part; the sums stay off the FP64 pipe.
+// All threads of the block take part; nothing runs on the FP64 pipe.
 template <int NT>
 __device__ __forceinline__ void cg_fold(CgState &s, const PcgScalars *sc, const float2 *partials, int nblk,
                                         float2 *sred) {
@@ -590,17 +619,13 @@ __device__ __forceinline__ void cg_fold(CgState &s, const PcgScalars *sc, const 
     block_sum_df<3>(tot, sred);
     if (threadIdx.x == 0) {
         int it = s.iter, done = 0, status = s.status;
-        double g = s.gamma, a = s.alpha, b = s.beta;
-        const double t0 = df_value(tot[0]), t1 = df_value(tot[1]), t2 = df_value(tot[2]);
-        cg_scalar_step(t0, t1, t2, sc->tol, sc->bnorm, sc->max_iter, it, done, status, g, a, b);
+        cg_scalar_step_df(tot[0], tot[1], tot[2], sc->rr_stop, sc->max_iter, it, done, status, s.gamma, s.alpha,
+                          s.beta);
         s.iter = it;
         s.done = done;
         s.status = status;
-        s.gamma = g;
-        s.alpha = a;
-        s.beta = b;
-        s.rr = t2;
-        s.pap = t1;
+        s.rr = tot[2];
+        s.pap = tot[1];
         s.pending = 0;
         sh = s;
     }
@@ -644,8 +669,8 @@ __global__ void __launch_bounds__(NT, 2)
                 ca.sc->st[par] = o;
             }
         }
-        alpha = (float)s.alpha;
-        beta = (float)s.beta;
+        alpha = s.alpha.hi;
+        beta = s.beta.hi;
         return !s.done;
     };
     float sums[3];

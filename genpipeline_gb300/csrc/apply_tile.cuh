@@ -29,8 +29,9 @@ enum { MODE_PLAIN = 0, MODE_PCG = 1, MODE_CG = 3, MODE_CG_FUSED = 4 };
 // State of the one-kernel PCG at the start of an iteration. Launch k writes slot k & 1 and
 // reads slot (k & 1) ^ 1; `pending` marks a state whose pass has written block partial sums
 // (slot k & 1 of the partials) that the next launch folds in before its own pass.
+// The scalars are double-float (hi, lo) pairs.
 struct CgState {
-    double alpha, beta, gamma, rr, pap;
+    df32 alpha, beta, gamma, rr, pap;
     int iter, done, status, pending;
 };
 
@@ -52,6 +53,7 @@ struct PcgScalars {
     int trips;        // WHILE-loop trips run by the device-driven loop
     int max_trips;    // hard cap on those trips (the loop always ends)
     int freeze;       // 1 = kernels leave the scalars as they are (timing of one pass)
+    float rr_stop;    // one-kernel PCG: (tol ||D b||)^2 in FP32, the stop test on r.r
     CgState st[2];    // one-kernel PCG: the state by launch parity
 };
 

@@ -146,10 +146,12 @@ __device__ __forceinline__ void block_sum_n(double (&v)[K], double *scratch) {
     }
 }
 
-// Double-float sums: a value hi + lo held as two FP32 numbers, added with the exact two-sum
-// error term (Knuth), about 48 significant bits. Used for the block and grid sums of the
-// PCG iteration, where FP64 adds would run on the narrow FP64 pipe. The add is commutative,
-// so butterfly reductions leave every lane with the same value.
+// Double-float arithmetic: a value hi + lo held as two FP32 numbers, about 44-48 significant
+// bits (Dekker 1971; Knuth's exact two-sum for the add). Used for the sums and the scalar
+// recurrence of the one-kernel PCG iteration, which sit on its critical path: on this part an
+// FP64 division takes about 550 cycles and an FP64 add or fma about 64, a double-float add
+// about 30. The add is commutative, so butterfly reductions leave every lane with the same
+// value.
 struct df32 {
     float hi, lo;
 };
@@ -163,6 +165,31 @@ __device__ __forceinline__ df32 df_add(df32 a, df32 b) {
     return df32{hi, lo};
 }
 __device__ __forceinline__ double df_value(df32 a) { return (double)a.hi + (double)a.lo; }
+__host__ __device__ __forceinline__ df32 df_from(double v) {
+    const float hi = (float)v;
+    return df32{hi, (float)(v - (double)hi)};
+}
+__device__ __forceinline__ df32 df_neg(df32 a) { return df32{-a.hi, -a.lo}; }
+// (a + b) renormalised, for |a| >= |b| (Dekker's fast two-sum).
+__device__ __forceinline__ df32 df_renorm(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return df32{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+// Product: the rounding error of a.hi * b.hi comes exactly from one fma (Dekker's product).
+__device__ __forceinline__ df32 df_mul(df32 a, df32 b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return df_renorm(p, e);
+}
+// Quotient by long division: the FP32 quotient of the leading parts, corrected once by the
+// quotient of the remainder a - q b.
+__device__ __forceinline__ df32 df_div(df32 a, df32 b) {
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const df32 r = df_add(a, df_neg(df_mul(df32{q1, 0.0f}, b)));
+    return df_renorm(q1, __fdiv_rn(r.hi, b.hi));
+}
 
 // K block sums in double-float with one pair of barriers; valid in thread 0. scratch: 32 K
 // float2.

@@ -246,8 +246,8 @@ __global__ void cg_start_kernel(int64_t nd, const float *__restrict__ w, const f
             CgState s = {};
             s.done = 1;
             s.status = sc->status;
-            s.rr = sc->rr;
-            s.gamma = sc->rz;
+            s.rr = df_from(sc->rr);
+            s.gamma = df_from(sc->rz);
             sc->st[1] = s;
         }
         return;
@@ -268,11 +268,13 @@ __global__ void cg_start_kernel(int64_t nd, const float *__restrict__ w, const f
             sc->alpha[0] = sc->rz / tot[0];
             sc->beta = 0.0;
         }
+        const double stop = sc->tol * sc->bnorm;
+        sc->rr_stop = (float)(stop * stop);
         CgState s = {};
-        s.alpha = sc->alpha[0];
-        s.gamma = sc->rz;
-        s.rr = sc->rr;
-        s.pap = tot[0];
+        s.alpha = df_from(sc->alpha[0]);
+        s.gamma = df_from(sc->rz);
+        s.rr = df_from(sc->rr);
+        s.pap = df_from(tot[0]);
         s.done = sc->done;
         s.status = sc->status;
         sc->st[1] = s;
@@ -289,11 +291,11 @@ __global__ void cg_fold_kernel(int nblk, int last, double *partials, PcgScalars 
     if (threadIdx.x == 0) {
         sc->st[last] = s;
         sc->iter = s.iter;
-        sc->rz = s.gamma;
-        sc->rr = s.rr;
-        sc->pap = s.pap;
-        sc->alpha[0] = s.alpha;
-        sc->beta = s.beta;
+        sc->rz = df_value(s.gamma);
+        sc->rr = df_value(s.rr);
+        sc->pap = df_value(s.pap);
+        sc->alpha[0] = df_value(s.alpha);
+        sc->beta = df_value(s.beta);
         if (sc->status == GBS_OK) sc->status = s.status;
         sc->done = sc->done || s.done;
     }
