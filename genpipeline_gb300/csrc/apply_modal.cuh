@@ -37,19 +37,29 @@ struct ModalGeom {
 };
 
 
-// Shared memory of the modal kernel for a given z extent (NT = 256, EPT = 2): three operand
-// planes of three component rows of R + 2 floats (rounded up to a multiple of 4), the raw
-// cp.async buffers (one per staged vector: p for the
-// plain apply; r, w, s, 1/diag, p, x for the PCG modes) and the output words of a plane,
-// each 4 * ceil((3R + 3) / 4) floats, two planes of element moduli, the y-direction slots
-// (3 floats per element) and the warp-boundary contributions (6 floats per warp and lane).
+// Row lengths of the shared-memory layout for R staged nodes per plane. A plane of R nodes
+// takes ceil((3R + 3) / 4) float4 groups, at most MAXV per thread. The MAXV = 2 kernels lay
+// out every R they take (R <= modal_r2) with the lengths of the largest one, so that the row
+// offsets are compile-time immediates; the MAXV = 3 kernels size the rows to R.
+template <int NT>
+__host__ __device__ constexpr int modal_r2() { return (8 * NT - 5) / 3; }
+__host__ __device__ constexpr int modal_rw(int R) { return 4 * ((3 * R + 6) / 4); }
+__host__ __device__ constexpr int modal_pr(int R) { return 4 * ((R + 5) / 4); }
+template <int NT>
+__host__ __device__ constexpr int modal_layout_r(int R) { return (3 * R + 6) / 4 <= 2 * NT ? modal_r2<NT>() : R; }
+
+// Shared memory of the modal kernel for a given z extent (NT = 256, EPT = 2): four operand
+// planes of three component rows of modal_pr floats (>= R + 2), the raw cp.async buffers of
+// modal_rw floats (one per staged vector: p for the plain apply; r, w, s, 1/diag, p, x for the
+// PCG modes), two planes of element moduli, and two copies (by step parity) of the y-direction
+// slots (3 floats per element) and of the warp-boundary contributions (6 floats per warp and
+// lane).
 template <int NT, int EPT>
 inline size_t modal_smem_bytes(int nz, bool cg) {
-    const int NE = NT * EPT, H = nz + 2, R = NE + H;
-    const size_t RW = 4 * (size_t)((3 * R + 6) / 4);
-    const size_t PR = 4 * (size_t)((R + 5) / 4);
-    return 9 * PR * sizeof(float) + ((cg ? 6 : 1) + 1) * RW * sizeof(float) +
-           (2 + 3) * (size_t)NT * sizeof(float2) + (size_t)(NT / 32) * 6 * sizeof(float2);
+    const int NE = NT * EPT, H = nz + 2, R = modal_layout_r<NT>(NE + H);
+    const size_t RW = (size_t)modal_rw(R), PR = (size_t)modal_pr(R);
+    return 12 * PR * sizeof(float) + (cg ? 6 : 1) * RW * sizeof(float) + (2 + 6) * (size_t)NT * sizeof(float2) +
+           2 * (size_t)(NT / 32) * 6 * sizeof(float2);
 }
 
 // cp.async (sm_80+): 16-byte global -> shared copies through L2 that use no registers;
@@ -206,18 +216,21 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     const int xs = seg * G.seglen;
     const int xe = min(xs + G.seglen, nx + 1);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int RW = 4 * ((3 * R + 6) / 4);
+    static_assert(MAXV == 2 || MAXV == 3, "two or three float4 groups per thread and plane");
+    const int RL = MAXV == 2 ? modal_r2<NT>() : R;  // layout rows (constant for MAXV = 2)
+    const int RW = modal_rw(RL);
     const int64_t NW = 3LL * (nx + 1) * S;  // words of a node vector
 
-    const int PR = 4 * ((R + 5) / 4);           // floats per component row (>= R + 2)
-    float *Pn = smem;                           // [3][3][PR] operand planes by component; node l at 1 + l
-    float *Raw = Pn + 9 * PR;                   // [NR][RW] cp.async buffers
-    float *Ys = Raw + NR * RW;                  // [RW] output words of the plane
-    float2 *Es2 = (float2 *)(Ys + RW);          // [2][NT] element moduli (tid, tid + NT)
-    float2 *Z1s = Es2 + 2 * NT;                 // [3][NT] y+1-side contributions (c) per element
-    float2 *Bd = Z1s + 3 * NT;                  // [NT/32][6] z+1-side contributions (cy, c) of lane 31
-    const float *Z1f = (const float *)Z1s;
-    const float *Bdf = (const float *)Bd;
+    const int PR = modal_pr(RL);                // floats per component row (>= R + 2)
+    // One barrier per plane step: the operand planes are a ring of four slots and the y-slots
+    // and warp-boundary terms alternate by step parity, so that a step's writes never meet
+    // the previous step's reads of the same buffer (a slot is rewritten two barriers after
+    // its last read).
+    float *Pn = smem;                           // [4][3][PR] operand planes by component; node l at 1 + l
+    float *Raw = Pn + 12 * PR;                  // [NR][RW] cp.async buffers
+    float2 *Es2 = (float2 *)(Raw + NR * RW);    // [2][NT] element moduli (tid, tid + NT)
+    float2 *Z1s = Es2 + 2 * NT;                 // [2][3][NT] y+1-side contributions (c) per element
+    float2 *Bd = Z1s + 6 * NT;                  // [2][NT/32][6] z+1-side contributions (cy, c) of lane 31
 
     float alpha = cp.alpha, beta = cp.beta;
     float g_ru = 0.0f, g_wu = 0.0f, g_rr = 0.0f;  // FP32 per-thread partials
@@ -377,25 +390,45 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     };
     float ex[EPT];
     bool eok[EPT];
+    // (y, z) offset ey nz + ez of element tid + q NT within an element plane, -1 outside the
+    // grid (loop-invariant: the integer division by NZ runs once per pass)
+    int eoff[EPT];
+#pragma unroll
+    for (int q = 0; q < EPT; ++q) {
+        const int ef = F0 - H + tid + q * NT;
+        const int ey = ef >= 0 ? ef / NZ : 0, ez = ef >= 0 ? ef - ey * NZ : 0;
+        eoff[q] = ef >= 0 && ey < ny && ez < nz ? ey * nz + ez : -1;
+    }
+    const int64_t eplane = (int64_t)ny * nz;
     auto issue_eplane = [&](int j) {
 #pragma unroll
         for (int q = 0; q < EPT; ++q) {
-            const int ef = F0 - H + tid + q * NT;
-            const int ey = ef >= 0 ? ef / NZ : 0, ez = ef >= 0 ? ef - ey * NZ : 0;
-            eok[q] = j >= 0 && j < nx && ef >= 0 && ey < ny && ez < nz;
-            ex[q] = eok[q] ? x[((int64_t)j * ny + ey) * nz + ez] : 0.0f;
+            eok[q] = j >= 0 && j < nx && eoff[q] >= 0;
+            ex[q] = eok[q] ? x[j * eplane + eoff[q]] : 0.0f;
         }
     };
     auto commit_eplane = [&](int slot) {
         Es2[slot * NT + tid] =
             make_float2(eok[0] ? modulus(law, ex[0]) : 0.0f, eok[1] ? modulus(law, ex[1]) : 0.0f);
     };
-    // z+1-side contribution (cy, c) of element e - 1 where e sits in lane 0
-    auto boundary = [&](int e, int cy, int c) -> float {
+    // Index in Bdf of the z+1-side contribution (cy, c = 0) of element e - 1, for an element e
+    // in lane 0; component c adds 2 c.
+    auto bd_index = [&](int e, int cy) -> int {
         const int pe = e - 1;
         const int pt = pe >= NT ? pe - NT : pe;
-        return Bdf[2 * ((pt >> 5) * 6 + cy * 3 + c) + (pe >= NT ? 1 : 0)];
+        return 2 * ((pt >> 5) * 6 + cy * 3) + (pe >= NT ? 1 : 0);
     };
+    // Node-phase terms of node l = tid + q NT that come from other warps (loop-invariant):
+    // bl[q] for lane 0 (element l - 1 in lane 31 of the previous warp), bm[q] for the node
+    // whose y-neighbour element m = l - NZ sits in lane 0; -1 where there is none.
+    int bl[EPT], bm[EPT];
+#pragma unroll
+    for (int q = 0; q < EPT; ++q) {
+        const int l = tid + q * NT, mm = l - NZ;
+        const bool node = l >= H;  // then l >= 1 and m >= 1
+        bl[q] = node && lane == 0 ? bd_index(l, 0) : -1;
+        bm[q] = node && (mm & 31) == 0 ? bd_index(mm, 1) : -1;
+    }
 
     // ---- prologue: node planes xs-1, xs and element plane xs-1 (the raw buffers hold one
     // plane: the second plane's copies go out after the first plane is combined) ----------
@@ -421,7 +454,8 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
 
     for (int i = xs - 1; i < xe; ++i) {  // modal_geom makes every segment non-empty
         const int k = i - (xs - 1);
-        const int s0 = k % 3, s1 = (k + 1) % 3, s2 = (k + 2) % 3;
+        const int s0 = k & 3, s1 = (k + 1) & 3, s2 = (k + 2) & 3;
+        float2 *Z1k = Z1s + (k & 1) * 3 * NT, *Bdk = Bd + (k & 1) * (NT / 32) * 6;
         const int es = k & 1;
         const bool more_nodes = i + 2 <= xe;
         const bool more_elems = i + 1 <= xe - 1;
@@ -475,21 +509,21 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
             float2 a1 = shfl_up2(h[1][c]), b1 = shfl_up2(h[3][c]);
             if (lane == 0) a1 = b1 = make_float2(0.0f, 0.0f);
             z0[c] = add2(h[0][c], a1);
-            Z1s[c * NT + tid] = add2(h[2][c], b1);
+            Z1k[c * NT + tid] = add2(h[2][c], b1);
         }
         if (lane == 31) {
 #pragma unroll
             for (int cy = 0; cy < 2; ++cy)
 #pragma unroll
-                for (int c = 0; c < 3; ++c) Bd[warp * 6 + cy * 3 + c] = h[cy * 2 + 1][c];
+                for (int c = 0; c < 3; ++c) Bdk[warp * 6 + cy * 3 + c] = h[cy * 2 + 1][c];
         }
         if (more_nodes) commit_plane(s2, i + 2);
         if (more_elems) commit_eplane(es ^ 1);
         __syncthreads();
 
-        // ---- nodes of plane i: node l = element l of this thread --------------------------
+        // ---- nodes of plane i: node l = element l of this thread, stored straight to y -----
         const float *Pu = Pn + s0 * 3 * PR + 1;
-        const PlaneW Pi = plane_w(i);
+        const float *Z1f = (const float *)Z1k, *Bdf = (const float *)Bdk;
 #pragma unroll
         for (int q = 0; q < EPT; ++q) {
             const int l = tid + q * NT;
@@ -498,37 +532,16 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                 const int m = l - NZ;  // element whose y+1 corners touch node l (m >= 1)
                 const int mi = m >= NT ? 2 * (m - NT) + 1 : 2 * m;
                 const float uc[3] = {Pu[l], Pu[PR + l], Pu[2 * PR + l]};
+                float *yo = y + 3 * ((int64_t)i * S + flat);
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     float s = (q ? z0[c].y : z0[c].x) + Z1f[c * 2 * NT + mi];
-                    if (lane == 0) s += boundary(l, 0, c);
-                    if ((m & 31) == 0) s += boundary(m, 1, c);
+                    const float tl = Bdf[max(bl[q], 0) + 2 * c], tm = Bdf[max(bm[q], 0) + 2 * c];
+                    s += bl[q] >= 0 ? tl : 0.0f;
+                    s += bm[q] >= 0 ? tm : 0.0f;
                     const float yc = ((om[q] >> c) & 1) ? 0.0f : s;
                     if (CG) g_wu = fmaf(uc[c], yc, g_wu);
-                    Ys[Pi.pad + 3 * l + c] = yc;
-                }
-            }
-        }
-        __syncthreads();
-
-        // ---- owned words of plane i out as float4 groups -----------------------------------
-        if (out_plane) {
-            const PlaneW &P = Pi;
-#pragma unroll
-            for (int q = 0; q < MAXV; ++q) {
-                const int f = tid + q * NT;
-                const int cw0 = 4 * f - P.pad;
-                if (f < P.nv && cw0 + 4 > P.olo3 && cw0 < P.ohi3) {
-                    const int64_t gw = P.A + 4 * (int64_t)f;
-                    const float4 y4 = *(const float4 *)(Ys + 4 * f);
-                    if (cw0 >= P.olo3 && cw0 + 4 <= P.ohi3) {
-                        *(float4 *)(y + gw) = y4;
-                    } else {
-                        const float yv[4] = {y4.x, y4.y, y4.z, y4.w};
-#pragma unroll
-                        for (int k = 0; k < 4; ++k)
-                            if (cw0 + k >= P.olo3 && cw0 + k < P.ohi3) y[gw + k] = yv[k];
-                    }
+                    yo[c] = yc;
                 }
             }
         }
