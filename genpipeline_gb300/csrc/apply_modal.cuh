@@ -553,41 +553,13 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
 }
 
 // The scalar step at the end of PCG iteration i, from gamma = r_{i+1}.u_{i+1},
-// delta = w_{i+1}.u_{i+1} and rho = r_{i+1}.r_{i+1} (all FP64). Returns the new state in
-// (it, done, status, gamma_i -> gamma, alpha, beta):
-//   stop when ||r_{i+1}|| < rtol ||D b|| (x_{i+1} is written), on a non-finite sum, or at
-//   max_iter; otherwise beta_{i+1} = gamma_{i+1} / gamma_i and
+// delta = w_{i+1}.u_{i+1} and rho = r_{i+1}.r_{i+1}, all in double-float. Returns the new
+// state in (it, done, status, gamma_i -> gamma, alpha, beta):
+//   stop when r.r < rr_stop = (rtol ||D b||)^2 (x_{i+1} is written; r.r = 0 also stops, for a
+//   threshold below the FP32 range), on a non-finite sum, or at max_iter; otherwise
+//   beta_{i+1} = gamma_{i+1} / gamma_i and
 //   alpha_{i+1} = gamma_{i+1} / (delta_{i+1} - beta_{i+1} gamma_{i+1} / alpha_i), whose
 //   denominator is p_{i+1}.A p_{i+1} (breakdown when it is not positive).
-__device__ __forceinline__ void cg_scalar_step(double gamma, double delta, double rho, double tol, double bnorm,
-                                               int max_iter, int &it, int &done, int &status, double &gamma_i,
-                                               double &alpha, double &beta) {
-    it += 1;
-    if (!isfinite(gamma) || !isfinite(delta) || !isfinite(rho)) {
-        done = 1;
-        status = GBS_ENONFINITE;
-    } else if (sqrt(rho) < tol * bnorm) {
-        done = 1;
-    } else if (it >= max_iter) {
-        done = 1;
-        status = GBS_ENOTCONV;
-    } else {
-        const double b1 = gamma / gamma_i;
-        const double den = delta - b1 * gamma / alpha;
-        if (!(den > 0.0)) {
-            done = 1;
-            status = GBS_EBREAKDOWN;
-        } else {
-            alpha = gamma / den;
-            beta = b1;
-            gamma_i = gamma;
-        }
-    }
-}
-
-// cg_scalar_step in double-float, for the one-kernel PCG: the same recurrence and stop
-// tests, with r.r compared against rr_stop = (tol ||D b||)^2 (no square root; r.r = 0 also
-// stops, for a threshold below the FP32 range).
 __device__ __forceinline__ void cg_scalar_step_df(df32 gamma, df32 delta, df32 rho, float rr_stop, int max_iter,
                                                   int &it, int &done, int &status, df32 &gamma_i, df32 &alpha,
                                                   df32 &beta) {

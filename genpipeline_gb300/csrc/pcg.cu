@@ -397,23 +397,23 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// Grid-wide sums at a barrier. Each block publishes its K block sums in slot `slot` (two
-// slots alternate: a block can only reach the next use of a slot after every block has left
-// the barrier that last read it), arrives on a monotonic counter and waits for `target`
-// arrivals; then every block sums all partials itself in block order, so every block holds
-// the same totals (no serial finisher, deterministic). Waits are bounded by wait_ns.
+// Grid-wide sums at a barrier, in double-float. Each block publishes its K block sums in
+// slot `slot` (two slots alternate: a block can only reach the next use of a slot after every
+// block has left the barrier that last read it), arrives on a monotonic counter and waits for
+// `target` arrivals; then every block sums all partials itself in block order, so every block
+// holds the same totals (no serial finisher, deterministic). Waits are bounded by wait_ns.
 template <int K>
-__device__ bool grid_sums(const double (&v)[K], double *partials, int slot, unsigned *count, unsigned target, int nblk,
-                          int bid, unsigned long long wait_ns, double *sred, double (&tot)[K]) {
+__device__ bool grid_sums(const float (&v)[K], float2 *partials, int slot, unsigned *count, unsigned target, int nblk,
+                          int bid, unsigned long long wait_ns, float2 *sred, df32 (&tot)[K]) {
     __shared__ bool s_ok;
-    double bs[K];
+    df32 bs[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) bs[k] = v[k];
-    block_sum_n<K>(bs, sred);
-    double *part = partials + (size_t)slot * K * nblk;
+    for (int k = 0; k < K; ++k) bs[k] = df32{v[k], 0.0f};
+    block_sum_df<K>(bs, sred);
+    float2 *part = partials + (size_t)slot * K * nblk;
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < K; ++k) part[k * nblk + bid] = bs[k];
+        for (int k = 0; k < K; ++k) part[k * nblk + bid] = make_float2(bs[k].hi, bs[k].lo);
         __threadfence();
         atomicAdd(count, 1u);
         s_ok = true;
@@ -429,14 +429,17 @@ __device__ bool grid_sums(const double (&v)[K], double *partials, int slot, unsi
     }
     __syncthreads();
     if (!s_ok) return false;
-    double s[K];
+    df32 s[K];
 #pragma unroll
-    for (int k = 0; k < K; ++k) s[k] = 0.0;
+    for (int k = 0; k < K; ++k) s[k] = df32{0.0f, 0.0f};
     for (int i = threadIdx.x; i < nblk; i += blockDim.x)
 #pragma unroll
-        for (int k = 0; k < K; ++k) s[k] += __ldcg(&part[k * nblk + i]);
-    block_sum_n<K>(s, sred);
-    __shared__ double s_tot[K];
+        for (int k = 0; k < K; ++k) {
+            const float2 w = __ldcg(&part[k * nblk + i]);
+            s[k] = df_add(s[k], df32{w.x, w.y});
+        }
+    block_sum_df<K>(s, sred);
+    __shared__ df32 s_tot[K];
     if (threadIdx.x == 0)
 #pragma unroll
         for (int k = 0; k < K; ++k) s_tot[k] = s[k];
@@ -452,14 +455,14 @@ __device__ bool grid_sums(const double (&v)[K], double *partials, int slot, unsi
 // arrivals, so each block's bounded wait expires and the kernel records GBS_ETIMEOUT.
 __global__ void barrier_selftest_kernel(double *partials, unsigned *count, int *status, unsigned extra,
                                         unsigned long long wait_ns) {
-    __shared__ double sred[32];
-    const double v[1] = {threadIdx.x == 0 ? 1.0 : 0.0};  // 1.0 per block
-    double tot[1];
-    const bool ok = grid_sums<1>(v, partials, 0, count, gridDim.x + extra, (int)gridDim.x, (int)blockIdx.x, wait_ns,
-                                 sred, tot);
+    __shared__ float2 sred[32];
+    const float v[1] = {threadIdx.x == 0 ? 1.0f : 0.0f};  // 1.0 per block
+    df32 tot[1];
+    const bool ok = grid_sums<1>(v, (float2 *)partials, 0, count, gridDim.x + extra, (int)gridDim.x, (int)blockIdx.x,
+                                 wait_ns, sred, tot);
     if (threadIdx.x == 0) {
         if (!ok) atomicExch(status, (int)GBS_ETIMEOUT);
-        else if (tot[0] != (double)gridDim.x) atomicExch(status, (int)GBS_EINVAL);
+        else if (df_value(tot[0]) != (double)gridDim.x) atomicExch(status, (int)GBS_EINVAL);
     }
 }
 
@@ -484,7 +487,7 @@ __global__ void __launch_bounds__(NT, 2)
     pcg_fused_kernel(const __grid_constant__ FusedTable T, Law<float> law, const ModalK km,
                      unsigned long long wait_ns) {
     extern __shared__ float4 smem4[];
-    __shared__ double sred[3 * 32];
+    __shared__ float2 sred[3 * 32];
     int di = 0;
     while (di + 1 < T.n && (int)blockIdx.x >= T.d[di + 1].block0) ++di;
     const FusedDesign &D = T.d[di];
@@ -496,28 +499,30 @@ __global__ void __launch_bounds__(NT, 2)
     PcgScalars *sc = ca.sc;
     // The solve's scalars, identical in every block of the design (each block computes them).
     const volatile PcgScalars *vsc = sc;
+    // Scalars in double-float (cg_scalar_step_df), as in the one-kernel-per-iteration form.
     int it = vsc->iter, done = vsc->done, status = vsc->status;
-    double gamma_i = vsc->rz, alpha = vsc->alpha[0], beta = vsc->beta, rr = vsc->rr, delta = vsc->pap;
-    const double tol = vsc->tol, bnorm = vsc->bnorm;
+    df32 gamma_i = df_from(vsc->rz), alpha = df_from(vsc->alpha[0]), beta = df_from(vsc->beta);
+    df32 rr = df_from(vsc->rr), delta = df_from(vsc->pap);
+    const double stop = vsc->tol * vsc->bnorm;
+    const float rr_stop = (float)(stop * stop);
     const int max_iter = vsc->max_iter;
     unsigned target = 0;
     while (!done) {
         const int c = it & 1, nc = c ^ 1;
-        const CgPass cp{(float)alpha, (float)beta, ca.r[c], ca.w[c], ca.s[nc], ca.dinv, ca.r[nc], ca.s[c], ca.p, ca.xu};
+        const CgPass cp{alpha.hi, beta.hi, ca.r[c], ca.w[c], ca.s[nc], ca.dinv, ca.r[nc], ca.s[c], ca.p, ca.xu};
         float sums[3];
         modal_pass<NT, EPT, MAXV, MODE_CG_FUSED>(G, D.x, nullptr, ca.w[nc], D.mask, law, km, cp, (float *)smem4, tile, seg,
                                                  sums, [](float &, float &) { return true; });
         __threadfence();
         target += nblk;
-        double tot[3];
-        const double v[3] = {(double)sums[0], (double)sums[1], (double)sums[2]};
-        if (!grid_sums<3>(v, ca.partials, it & 1, &sc->bar_count, target, nblk, bid, wait_ns, sred, tot)) {
+        df32 tot[3];
+        if (!grid_sums<3>(sums, (float2 *)ca.partials, it & 1, &sc->bar_count, target, nblk, bid, wait_ns, sred, tot)) {
             status = GBS_ETIMEOUT;
             break;
         }
         rr = tot[2];
         delta = tot[1];
-        cg_scalar_step(tot[0], tot[1], tot[2], tol, bnorm, max_iter, it, done, status, gamma_i, alpha, beta);
+        cg_scalar_step_df(tot[0], tot[1], tot[2], rr_stop, max_iter, it, done, status, gamma_i, alpha, beta);
     }
     if (status == GBS_ETIMEOUT) {
         if (threadIdx.x == 0) {
@@ -530,11 +535,11 @@ __global__ void __launch_bounds__(NT, 2)
         sc->iter = it;
         sc->done = 1;
         sc->status = status;
-        sc->rz = gamma_i;
-        sc->rr = rr;
-        sc->pap = delta;
-        sc->alpha[0] = alpha;
-        sc->beta = beta;
+        sc->rz = df_value(gamma_i);
+        sc->rr = df_value(rr);
+        sc->pap = df_value(delta);
+        sc->alpha[0] = df_value(alpha);
+        sc->beta = df_value(beta);
     }
 }
 
