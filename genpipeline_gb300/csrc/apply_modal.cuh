@@ -179,6 +179,7 @@ struct CgPass {
     float alpha, beta;
     const float *r, *w, *sold, *dinv;
     float *rnew, *snew, *p, *xu;
+    float *clear;  // MODE_CG: the next launch's output w (its shared node planes are zeroed here)
 };
 
 template <int MODE>
@@ -193,6 +194,16 @@ __device__ __forceinline__ float ld_vec(const float *p) {
 // aligned. pre(alpha, beta) runs once the first plane's copies are in flight (the step's
 // scalars can be formed meanwhile); when it returns false the pass stops there (returns
 // false).
+//
+// Segments. PLAIN and CG_FUSED: segment s owns node planes [xs, xe) of nx + 1 and also
+// computes element plane xs - 1 (a halo step) so that every owned node sums all its elements.
+// CG: segment s computes element planes [xs, xe) of nx, owns node planes [xs, xe) (the last
+// segment also node plane nx) and outputs node planes xs..xe. Node plane xs of s > 0 and node
+// plane xe < nx each get one half from this segment and one from its neighbour; both add
+// their halves into y, which the launch before cleared on those planes (cp.clear). Two
+// additions onto zero give the same result in either order, so the sum stays deterministic,
+// and the w.u shares add up the same way. That saves the halo step's element work and one
+// staged plane per CTA.
 template <int NT, int EPT, int MAXV, int MODE, typename Pre>
 __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__restrict__ x,
                                            const float *__restrict__ p, float *__restrict__ y,
@@ -213,8 +224,11 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     const int R = NE + H;         // staged nodes per plane
     const int F = NE - H;         // owned nodes per plane (chunk positions [H, NE))
     const int F0 = tile * F;
+    constexpr bool EDGE = MODE == MODE_CG;
     const int xs = seg * G.seglen;
-    const int xe = min(xs + G.seglen, nx + 1);
+    const int xe = min(xs + G.seglen, EDGE ? nx : nx + 1);
+    const int own_hi = (EDGE && xe == nx) ? nx + 1 : xe;  // owned node planes [xs, own_hi)
+    const int x0 = EDGE ? xs : xs - 1;                     // first element plane of the pass
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     static_assert(MAXV == 2 || MAXV == 3, "two or three float4 groups per thread and plane");
     const int RL = MAXV == 2 ? modal_r2<NT>() : R;  // layout rows (constant for MAXV = 2)
@@ -256,7 +270,7 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
         P.pv = j >= 0 && j <= nx;
         P.lo3 = 3 * max(0, H - F0);          // chunk words of nodes inside the plane
         P.hi3 = 3 * min(R, S - F0 + H);
-        P.own = j >= xs && j < xe;
+        P.own = j >= xs && j < own_hi;
         P.olo3 = 3 * H;                      // chunk words of owned nodes
         P.ohi3 = 3 * min(NE, S - F0 + H);
         return P;
@@ -388,6 +402,26 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
             }
         }
     };
+    // Zeroes this CTA's owned words of node plane j in cp.clear (MODE_CG: a shared plane of the
+    // next launch's output).
+    auto clear_plane = [&](int j) {
+        const PlaneW P = plane_w(j);
+#pragma unroll
+        for (int q = 0; q < MAXV; ++q) {
+            const int f = tid + q * NT;
+            const int cw0 = 4 * f - P.pad;
+            if (f < P.nv && cw0 + 4 > P.olo3 && cw0 < P.ohi3) {
+                const int64_t gw = P.A + 4 * (int64_t)f;
+                if (cw0 >= P.olo3 && cw0 + 4 <= P.ohi3) {
+                    *(float4 *)(cp.clear + gw) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        if (cw0 + k >= P.olo3 && cw0 + k < P.ohi3) cp.clear[gw + k] = 0.0f;
+                }
+            }
+        }
+    };
     float ex[EPT];
     bool eok[EPT];
     // (y, z) offset ey nz + ez of element tid + q NT within an element plane, -1 outside the
@@ -430,18 +464,19 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
         bm[q] = node && (mm & 31) == 0 ? bd_index(mm, 1) : -1;
     }
 
-    // ---- prologue: node planes xs-1, xs and element plane xs-1 (the raw buffers hold one
+    // ---- prologue: node planes x0, x0 + 1 and element plane x0 (the raw buffers hold one
     // plane: the second plane's copies go out after the first plane is combined) ----------
-    issue_plane(xs - 1);
-    issue_eplane(xs - 1);
+    issue_plane(x0);
+    issue_eplane(x0);
     if (!pre(alpha, beta)) {
         cp_async_wait_all();  // no copy may land after the CTA has left
         return false;
     }
-    commit_plane(0, xs - 1);
-    issue_plane(xs);
+    commit_plane(0, x0);
+    issue_plane(x0 + 1);
     commit_eplane(0);
-    commit_plane(1, xs);
+    commit_plane(1, x0 + 1);
+    if (EDGE && xs > 0) clear_plane(xs);
     __syncthreads();
 
     // x-direction carry: the cx = 1 half of element plane i - 1 in the (y, z) modal basis,
@@ -452,8 +487,11 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
 #pragma unroll
         for (int c = 0; c < 3; ++c) g1[b][c] = make_float2(0.0f, 0.0f);
 
-    for (int i = xs - 1; i < xe; ++i) {  // modal_geom makes every segment non-empty
-        const int k = i - (xs - 1);
+    // steps x0..xlast: element plane i (while i < xe, or i < nx with a halo step) and node
+    // plane i out (from xs on)
+    const int xlast = EDGE ? xe : xe - 1;
+    for (int i = x0; i <= xlast; ++i) {  // modal_geom makes every segment non-empty
+        const int k = i - x0;
         const int s0 = k & 3, s1 = (k + 1) & 3, s2 = (k + 2) & 3;
         float2 *Z1k = Z1s + (k & 1) * 3 * NT, *Bdk = Bd + (k & 1) * (NT / 32) * 6;
         const int es = k & 1;
@@ -461,7 +499,8 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
         const bool more_elems = i + 1 <= xe - 1;
         if (more_nodes) issue_plane(i + 2);
         if (more_elems) issue_eplane(i + 1);
-        const bool out_plane = i >= xs;
+        const bool out_plane = EDGE || i >= xs;
+        const bool shared = EDGE && ((i == xs && xs > 0) || (i == xe && xe < nx));  // added, not stored
         uint8_t om[EPT];
 #pragma unroll
         for (int q = 0; q < EPT; ++q) {
@@ -474,7 +513,7 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
         // h: the contributions of element planes i - 1 (carried) and i to node plane i, summed
         // in the (y, z) modal basis, then transformed back
         float2 h[4][3];
-        if (i >= 0 && i < nx) {
+        if (EDGE ? i < xe : (i >= 0 && i < nx)) {
             const float2 E = Es2[es * NT + tid];
             float2 v[8][3];
 #pragma unroll
@@ -541,7 +580,10 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                     s += bm[q] >= 0 ? tm : 0.0f;
                     const float yc = ((om[q] >> c) & 1) ? 0.0f : s;
                     if (CG) g_wu = fmaf(uc[c], yc, g_wu);
-                    yo[c] = yc;
+                    if (shared)
+                        atomicAdd(yo + c, yc);
+                    else
+                        yo[c] = yc;
                 }
             }
         }
@@ -618,27 +660,33 @@ __device__ __forceinline__ void cg_fold(CgState &s, const PcgScalars *sc, const 
     s = sh;
 }
 
-// par: launch parity (k & 1 for the k-th launch of a solve; the graph loop and the host loops
-// know it statically). MODE_CG reads state slot par ^ 1 and partial slot par ^ 1, writes
-// state slot par (block 0) and partial slot par.
+// phase: k mod 6 for the k-th launch of a solve (the graph loop and the host loops know it
+// statically); par = k & 1. MODE_CG reads state slot par ^ 1 and partial slot par ^ 1, writes
+// state slot par (block 0) and partial slot par; w rotates by k mod 3 (CgArgs).
 template <int NT, int EPT, int MAXV, int MODE>
 __global__ void __launch_bounds__(NT, 2)
     apply_modal_kernel(ModalGeom G, const float *__restrict__ x, const float *__restrict__ p, float *__restrict__ y,
-                       const uint8_t *__restrict__ mask, Law<float> law, const ModalK km, CgArgs ca, int par) {
+                       const uint8_t *__restrict__ mask, Law<float> law, const ModalK km, CgArgs ca, int phase) {
     extern __shared__ float4 smem4[];
     __shared__ float2 sred[3 * 32];
     const int tid = threadIdx.x;
     const int nblk = gridDim.x * gridDim.y;
     const int bid = blockIdx.x + gridDim.x * blockIdx.y;
-    CgPass cp{0.0f, 0.0f, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    const int par = phase & 1;
+    CgPass cp{0.0f, 0.0f, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     if (MODE == MODE_CG) {
         // Launch k runs iteration k while the solve lasts, so the vector parity is the launch
-        // parity: the first plane's copies go out before the state is known.
-        const bool odd = par;  // parity selects (a dynamic index into the parameter arrays would copy them to the stack)
+        // parity (and w cycles with k mod 3): the first plane's copies go out before the state
+        // is known. Selects, not dynamic indices (those would copy the parameter arrays to the
+        // stack).
+        const bool odd = par;
+        const int w3 = phase >= 3 ? phase - 3 : phase;
         float *r_c = odd ? ca.r[1] : ca.r[0], *r_n = odd ? ca.r[0] : ca.r[1];
-        float *w_c = odd ? ca.w[1] : ca.w[0], *w_n = odd ? ca.w[0] : ca.w[1];
         float *s_c = odd ? ca.s[1] : ca.s[0], *s_n = odd ? ca.s[0] : ca.s[1];
-        cp = CgPass{0.0f, 0.0f, r_c, w_c, s_n, ca.dinv, r_n, s_c, ca.p, ca.xu};
+        float *w_c = w3 == 0 ? ca.w[0] : w3 == 1 ? ca.w[1] : ca.w[2];
+        float *w_n = w3 == 0 ? ca.w[1] : w3 == 1 ? ca.w[2] : ca.w[0];
+        float *w_z = w3 == 0 ? ca.w[2] : w3 == 1 ? ca.w[0] : ca.w[1];
+        cp = CgPass{0.0f, 0.0f, r_c, w_c, s_n, ca.dinv, r_n, s_c, ca.p, ca.xu, w_z};
         y = w_n;
     }
     auto pre = [&](float &alpha, float &beta) -> bool {
@@ -679,18 +727,21 @@ constexpr int kModalEPT = 2;
 
 inline bool modal_fits(int nz) { return nz + 2 <= kModalNT * kModalEPT - 64 && nz + 2 <= 2 * kModalNT; }
 
-inline ModalGeom modal_geom(int nx, int ny, int nz, int num_sms, int blocks_per_sm) {
+// edge: segments over the nx element planes (MODE_CG, shared boundary node planes), else
+// over the nx + 1 node planes (a halo element plane per segment).
+inline ModalGeom modal_geom(int nx, int ny, int nz, int num_sms, int blocks_per_sm, bool edge = false) {
     const int NE = kModalNT * kModalEPT, H = nz + 2, F = NE - H;
     const int S = (ny + 1) * (nz + 1);
     const int tiles = (S + F - 1) / F;
+    const int planes = edge ? nx : nx + 1;
     const int target = (num_sms > 0 ? num_sms : 148) * (blocks_per_sm > 0 ? blocks_per_sm : 1);
     // As many x segments as fit in one wave of resident CTAs (rounding down, so that the
     // re-rounded segment count never exceeds the target).
     int nseg = target / tiles;
-    if (nseg > nx + 1) nseg = nx + 1;
+    if (nseg > planes) nseg = planes;
     if (nseg < 1) nseg = 1;
-    const int seglen = (nx + 1 + nseg - 1) / nseg;
-    nseg = (nx + 1 + seglen - 1) / seglen;
+    const int seglen = (planes + nseg - 1) / nseg;
+    nseg = (planes + seglen - 1) / seglen;
     ModalGeom g{nx, ny, nz, nseg, seglen};
     return g;
 }
@@ -750,25 +801,26 @@ template <int MODE>
 inline int modal_blocks(const gbsimp_ctx *ctx, int nx, int ny, int nz) {
     const int per_sm = modal_prepare<MODE>(ctx, nz);
     if (per_sm < 0) return per_sm;
-    const dim3 g = modal_grid(modal_geom(nx, ny, nz, ctx->num_sms, per_sm));
+    const dim3 g = modal_grid(modal_geom(nx, ny, nz, ctx->num_sms, per_sm, MODE == MODE_CG));
     return (int)(g.x * g.y);
 }
 
-// Launches the modal kernel (MODE_PLAIN: y = D K D p; MODE_CG: one PCG iteration).
+// Launches the modal kernel (MODE_PLAIN: y = D K D p; MODE_CG: one PCG iteration, phase =
+// launch index mod 6).
 template <int MODE>
 inline int launch_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
                         const float *p, float *y, const uint8_t *mask, const CgArgs &ca, cudaStream_t st,
-                        int par = 0) {
+                        int phase = 0) {
     const int per_sm = modal_prepare<MODE>(ctx, nz);
     if (per_sm < 0) return -per_sm;
     const size_t smem = modal_smem_bytes<kModalNT, kModalEPT>(nz, MODE != MODE_PLAIN);
-    const ModalGeom g = modal_geom(nx, ny, nz, ctx->num_sms, per_sm);
+    const ModalGeom g = modal_geom(nx, ny, nz, ctx->num_sms, per_sm, MODE == MODE_CG);
     if (modal_short(nz))
         apply_modal_kernel<kModalNT, kModalEPT, 2, MODE>
-            <<<modal_grid(g), kModalNT, smem, st>>>(g, x, p, y, mask, law, ctx->km, ca, par);
+            <<<modal_grid(g), kModalNT, smem, st>>>(g, x, p, y, mask, law, ctx->km, ca, phase);
     else
         apply_modal_kernel<kModalNT, kModalEPT, 3, MODE>
-            <<<modal_grid(g), kModalNT, smem, st>>>(g, x, p, y, mask, law, ctx->km, ca, par);
+            <<<modal_grid(g), kModalNT, smem, st>>>(g, x, p, y, mask, law, ctx->km, ca, phase);
     GBS_LAUNCH_CHECK("apply_modal_kernel");
     return GBS_OK;
 }

@@ -71,7 +71,9 @@ struct PcgArgs {
 // s[(i+1)&1] and writes r[(i+1)&1], w[(i+1)&1], s[i&1]; p and x are updated in place.
 struct CgArgs {
     float *r[2];        // r_i (masked residual)
-    float *w[2];        // w_i = D K D u_i, u_i = M r_i
+    float *w[3];        // w_i = D K D u_i, u_i = M r_i: launch k reads w[k % 3], writes w[(k + 1) % 3]
+                        // and clears the shared node planes of w[(k + 2) % 3], the next launch's
+                        // output (the persistent kernel uses w[0], w[1] by iteration parity)
     float *s[2];        // s_i = D K D p_i
     float *p;           // search direction
     float *xu;          // iterate

@@ -42,10 +42,10 @@ static inline unsigned vec_blocks(const gbsimp_ctx *ctx, int64_t n) {
 
 // ---- workspace of the FP32 PCG -----------------------------------------------------------
 // Dense form: r, dinv, p0/p1 (p_k in p[k&1]), ap. Single-reduction form: r/r1 (r[i&1]),
-// ap/p1 (w[i&1]), s0/s1 (s[i&1]), p0 (p), dinv.
+// ap/p1/w2 (w[i%3]; the persistent kernel w[i&1]), s0/s1 (s[i&1]), p0 (p), dinv.
 struct PcgWs {
     PcgScalars *sc;
-    float *r, *dinv, *p0, *p1, *ap, *r1, *s0, *s1;
+    float *r, *dinv, *p0, *p1, *ap, *r1, *s0, *s1, *w2;
     double *partials;
     size_t partial_count;
 };
@@ -60,7 +60,7 @@ static size_t pcg_partials(int nx, int ny, int nz) {
 
 static size_t pcg_ws_bytes_impl(int nx, int ny, int nz) {
     const size_t nd = (size_t)n_dof_of(nx, ny, nz);
-    return 256 + al256(sizeof(PcgScalars)) + 8 * al256(nd * sizeof(float)) +
+    return 256 + al256(sizeof(PcgScalars)) + 9 * al256(nd * sizeof(float)) +
            al256(pcg_partials(nx, ny, nz) * sizeof(double));
 }
 
@@ -74,8 +74,8 @@ static PcgWs pcg_ws(void *ws, int nx, int ny, int nz) {
     PcgWs w;
     w.sc = (PcgScalars *)p;
     p += al256(sizeof(PcgScalars));
-    float **v[8] = {&w.r, &w.dinv, &w.p0, &w.p1, &w.ap, &w.r1, &w.s0, &w.s1};
-    for (int i = 0; i < 8; ++i) {
+    float **v[9] = {&w.r, &w.dinv, &w.p0, &w.p1, &w.ap, &w.r1, &w.s0, &w.s1, &w.w2};
+    for (int i = 0; i < 9; ++i) {
         *v[i] = (float *)p;
         p += al256(nd * sizeof(float));
     }
@@ -90,6 +90,7 @@ static CgArgs cg_args(const PcgWs &w, float *u) {
     a.r[1] = w.r1;
     a.w[0] = w.ap;
     a.w[1] = w.p1;
+    a.w[2] = w.w2;
     a.s[0] = w.s0;
     a.s[1] = w.s1;
     a.p = w.p0;
@@ -238,9 +239,10 @@ __global__ void cg_init_kernel(int64_t nd, const float *__restrict__ b, float *q
 }
 
 // Single-reduction setup, step 2 (after w_0 = D K D u_0): alpha_0 = (r_0.u_0) / (w_0.u_0),
-// beta_0 = 0.
-__global__ void cg_start_kernel(int64_t nd, const float *__restrict__ w, const float *__restrict__ u,
-                                double *partials, PcgScalars *sc) {
+// beta_0 = 0. u_0 (in w[1], no longer needed) is cleared as it is read: the first launch adds
+// its output into w[1] on the segments' shared node planes.
+__global__ void cg_start_kernel(int64_t nd, const float *__restrict__ w, float *__restrict__ u, double *partials,
+                                PcgScalars *sc) {
     if (sc->done) {  // the first launch reads state slot 1
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             CgState s = {};
@@ -253,8 +255,10 @@ __global__ void cg_start_kernel(int64_t nd, const float *__restrict__ w, const f
         return;
     }
     float wu = 0.0f;
-    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
         wu = fmaf(w[d], u[d], wu);
+        u[d] = 0.0f;
+    }
     __shared__ double tot[3];
     if (last_block3(wu, 0.0, 0.0, partials, &sc->counter, tot) && threadIdx.x == 0) {
         sc->pap = tot[0];
@@ -359,9 +363,9 @@ static int read_scalars(const PcgScalars *d, PcgScalars *h, cudaStream_t st) {
 // Launches one iteration: the single-reduction kernel (modal element) or K1 + K2.
 static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
                          const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st, cudaEvent_t after_k1,
-                         int par) {
+                         int phase) {
     if (use_modal(ctx, nz)) {
-        int rc = launch_modal<MODE_CG>(ctx, nx, ny, nz, law, x, nullptr, nullptr, mask, cg_args(w, u), st, par);
+        int rc = launch_modal<MODE_CG>(ctx, nx, ny, nz, law, x, nullptr, nullptr, mask, cg_args(w, u), st, phase);
         if (rc) return rc;
         if (after_k1) GBS_CUDA_TRY(cudaEventRecord(after_k1, st));
         return GBS_OK;
@@ -509,7 +513,7 @@ __global__ void __launch_bounds__(NT, 2)
     unsigned target = 0;
     while (!done) {
         const int c = it & 1, nc = c ^ 1;
-        const CgPass cp{alpha.hi, beta.hi, ca.r[c], ca.w[c], ca.s[nc], ca.dinv, ca.r[nc], ca.s[c], ca.p, ca.xu};
+        const CgPass cp{alpha.hi, beta.hi, ca.r[c], ca.w[c], ca.s[nc], ca.dinv, ca.r[nc], ca.s[c], ca.p, ca.xu, nullptr};
         float sums[3];
         modal_pass<NT, EPT, MAXV, MODE_CG_FUSED>(G, D.x, nullptr, ca.w[nc], D.mask, law, km, cp, (float *)smem4, tile, seg,
                                                  sums, [](float &, float &) { return true; });
@@ -649,7 +653,8 @@ static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n,
 // kernels return at once when done is set, so a finished solve costs at most kLoopUnroll-1
 // empty iterations. The condition kernel also counts trips and stops
 // the loop with GBS_ETIMEOUT after max_trips (set from max_iter), so the loop always ends.
-constexpr int kLoopUnroll = 8;
+constexpr int kLoopUnroll = 6;
+static_assert(kLoopUnroll % 6 == 0, "a trip must end on launch phase 5 (parity 1, w index 2)");
 
 static inline int launches_per_trip(const gbsimp_ctx *ctx, int nz) {
     return (use_modal(ctx, nz) ? 1 : 2) * kLoopUnroll + 1;
@@ -694,7 +699,7 @@ struct LoopKey {
 
 static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
                          const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st, cudaEvent_t after_k1,
-                         int par);
+                         int phase);
 
 // Publishes the state after one-kernel PCG launches (last launch of parity `last`).
 static int cg_publish(const gbsimp_ctx *ctx, int nx, int ny, int nz, const PcgWs &w, int last, cudaStream_t st) {
@@ -776,7 +781,7 @@ static int loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<f
         }
         set_capturing(true);
         for (int i = 0; i < kLoopUnroll && rc == GBS_OK; ++i)
-            rc = pcg_iteration(ctx, nx, ny, nz, law, x, mask, u, w, gc->cap, nullptr, i & 1);
+            rc = pcg_iteration(ctx, nx, ny, nz, law, x, mask, u, w, gc->cap, nullptr, i % 6);
         if (rc == GBS_OK) {
             pcg_loop_cond_kernel<<<1, 1, 0, gc->cap>>>(h, w.sc);
             e = cudaGetLastError();
@@ -906,7 +911,7 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
         for (int i = 0; i < n; ++i) {
             if (prof) GBS_CUDA_TRY(cudaEventRecord(ev[2 * i], st));
             rc = pcg_iteration(ctx, nx, ny, nz, law, x, mask, u, w, st, prof ? ev[2 * i + 1] : nullptr,
-                               (launched + i) & 1);
+                               (launched + i) % 6);
             if (rc) return rc;
         }
         launched += n;
@@ -1314,6 +1319,7 @@ extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, co
         fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.s0);
         fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.s1);
         fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.p0);
+        fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.w2);
         freeze_scalars_kernel<<<1, 1, 0, st>>>(w.sc);
     }
     GBS_LAUNCH_CHECK("time_pcg_apply setup");
@@ -1331,7 +1337,7 @@ extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, co
     for (int i = 0; i < reps && rc == GBS_OK; ++i) {
         if (modal) {
             rc = launch_modal<MODE_CG>(ctx, nx, ny, nz, law, x, nullptr, nullptr, node_mask, cg_args(w, xu), gc->cap,
-                                       i & 1);
+                                       i % 6);
         } else {
             TileArgs<float> A{nx, ny, nz, x, nullptr, w.ap, node_mask};
             const dim3 g = tile_grid<TileF>(nx, ny, nz), b = tile_block<TileF>();
