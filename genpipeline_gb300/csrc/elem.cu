@@ -352,41 +352,137 @@ __global__ void oc_init_kernel(int64_t n, const OcParams P, const float *__restr
     }
 }
 
-// One bisection step (simp_solver.py:229-247). Every block evaluates the same tolerance
-// test on (l1, l2); when it holds, the step only records lfinal.
-__global__ void __launch_bounds__(256) oc_step_kernel(int64_t n, const OcParams P, const float *__restrict__ x,
-                                                      const float *__restrict__ dc, const uint8_t *__restrict__ pres,
-                                                      const float *__restrict__ w, double *partials,
-                                                      OcScalars *sc) {
-    __shared__ double sred[32];
-    __shared__ double tot[1];
+// ---- multisection: kOcLevels bisection steps per launch ---------------------------------
+// The bisection of simp_solver.py:229-247 visits one midpoint per step. One launch evaluates
+// the volume at every midpoint the next kOcLevels steps could visit: the 2^kOcLevels - 1 nodes
+// of the binary tree below (l1, l2), heap-ordered (node t: children 2t + 1 = [lo, mid] and
+// 2t + 2 = [mid, hi]), each midpoint formed as bisection forms it, 0.5 (hi + lo) of its
+// parent interval. The last block then walks the tree with bisection's tests (stop on
+// (l2 - l1) / (l1 + l2 + eps) < tol, then vol > volfrac -> l1 = mid, else l2 = mid), so the
+// sequence of intervals, lfinal and the step count are those of one launch per step (up to
+// the rounding of the volume sums), in max_bisect / kOcLevels launches.
+constexpr int kOcLevels = 5;
+constexpr int kOcNodes = (1 << kOcLevels) - 1;
+constexpr int kOcThreads = 256;
+
+__global__ void __launch_bounds__(kOcThreads) oc_multi_kernel(int64_t n, const OcParams P, const float *__restrict__ x,
+                                                              const float *__restrict__ dc,
+                                                              const uint8_t *__restrict__ pres,
+                                                              const float *__restrict__ w, float2 *partials,
+                                                              OcScalars *sc) {
+    __shared__ float s_sq[kOcNodes];    // sqrt(1 / mid) of node t
+    __shared__ bool s_stop[kOcNodes];   // the stop test on node t's interval
+    __shared__ double s_mid[kOcNodes];  // midpoint of node t
+    __shared__ float s_part[kOcNodes][kOcThreads];
+    __shared__ double s_tot[kOcNodes];
+    __shared__ bool s_last;
     if (sc->done) return;
-    const double l1 = sc->l1, l2 = sc->l2;
-    const double lmid = 0.5 * (l2 + l1);
-    if ((l2 - l1) / (l1 + l2 + P.tol_eps) < P.tol) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            sc->lfinal = lmid;
-            sc->steps += 1;
-            sc->done = 1;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nblk = gridDim.x;
+    if (tid < kOcNodes) {  // node tid: follow its path from the root (bits of tid + 1 below the leading one)
+        double lo = sc->l1, hi = sc->l2;
+        const int path = tid + 1, depth = 31 - __clz(path);
+        for (int i = depth - 1; i >= 0; --i) {
+            const double m = 0.5 * (hi + lo);
+            if ((path >> i) & 1)
+                lo = m;
+            else
+                hi = m;
         }
-        return;
+        const double m = 0.5 * (hi + lo);
+        s_mid[tid] = m;
+        s_sq[tid] = (float)sqrt(1.0 / m);
+        s_stop[tid] = (hi - lo) / (lo + hi + P.tol_eps) < P.tol;
     }
-    const float inv_l = (float)(1.0 / lmid);
-    float v = 0.0f;  // per-thread FP32 partial (a few terms), FP64 block and grid sums
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-        // Preserved elements hold xnew = 1 and still feed their neighbours' filtered density.
-        v = fmaf(w[e], oc_trial(x[e], dc[e], inv_l, P, pres && pres[e]), v);
+    __syncthreads();
+    // trial density of node t: x sqrt(max(-dc / mid, floor)) clamped, written as
+    // x max(sqrt(-dc) sqrt(1 / mid), sqrt(floor)) (sqrt is monotone: one square root per element)
+    float sq[kOcNodes], v[kOcNodes];
+#pragma unroll
+    for (int t = 0; t < kOcNodes; ++t) {
+        sq[t] = s_sq[t];
+        v[t] = 0.0f;
     }
-    const double vv[1] = {(double)v};
-    if (last_block_reduce<1>(vv, partials, &sc->counter, tot, sred) && threadIdx.x == 0) {
-        const double vol = (tot[0] + sc->npres) / (double)n;
-        if (vol > P.volfrac)
-            sc->l1 = lmid;
-        else
-            sc->l2 = lmid;
-        sc->lfinal = lmid;
-        sc->steps += 1;
-        if (sc->steps >= P.max_bisect) sc->done = 1;
+    const float sfloor = sqrtf(P.sqrt_floor);
+    for (int64_t e = blockIdx.x * (int64_t)kOcThreads + tid; e < n; e += (int64_t)nblk * kOcThreads) {
+        const float we = w[e];
+        if (pres && pres[e]) {  // xnew = 1
+#pragma unroll
+            for (int t = 0; t < kOcNodes; ++t) v[t] += we;
+            continue;
+        }
+        const float xe = x[e], s0 = sqrtf(fmaxf(-dc[e], 0.0f));
+        const float lo = xe - P.move, hi = xe + P.move;
+#pragma unroll
+        for (int t = 0; t < kOcNodes; ++t) {
+            float tv = xe * fmaxf(s0 * sq[t], sfloor);
+            tv = fminf(fmaxf(tv, 0.0f), 1.0f);
+            tv = fminf(fmaxf(tv, lo), hi);
+            v[t] = fmaf(we, tv, v[t]);
+        }
+    }
+    // block sums: warp wi sums nodes wi, wi + 8, ... over the block's threads in double-float
+#pragma unroll
+    for (int t = 0; t < kOcNodes; ++t) s_part[t][tid] = v[t];
+    __syncthreads();
+    for (int t = warp; t < kOcNodes; t += kOcThreads / 32) {
+        df32 a{0.0f, 0.0f};
+        for (int j = lane; j < kOcThreads; j += 32) a = df_add(a, df32{s_part[t][j], 0.0f});
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            a = df_add(a, df32{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)});
+        if (lane == 0) partials[t * nblk + blockIdx.x] = make_float2(a.hi, a.lo);
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&sc->counter, 1u) == (unsigned)nblk - 1;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    for (int t = warp; t < kOcNodes; t += kOcThreads / 32) {
+        df32 a{0.0f, 0.0f};
+        for (int b = lane; b < nblk; b += 32) {
+            const float2 p = __ldcg(&partials[t * nblk + b]);
+            a = df_add(a, df32{p.x, p.y});
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            a = df_add(a, df32{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)});
+        if (lane == 0) s_tot[t] = df_value(a);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double l1 = sc->l1, l2 = sc->l2, lfinal = sc->lfinal;
+        int steps = sc->steps, done = 0, node = 0;
+        const double target = P.volfrac * (double)n - sc->npres;  // vol > volfrac <=> sum > target
+        for (int lvl = 0; lvl < kOcLevels; ++lvl) {
+            const double m = s_mid[node];
+            if (s_stop[node]) {
+                lfinal = m;
+                steps += 1;
+                done = 1;
+                break;
+            }
+            if (s_tot[node] > target) {
+                l1 = m;
+                node = 2 * node + 2;
+            } else {
+                l2 = m;
+                node = 2 * node + 1;
+            }
+            lfinal = m;
+            steps += 1;
+            if (steps >= P.max_bisect) {
+                done = 1;
+                break;
+            }
+        }
+        sc->l1 = l1;
+        sc->l2 = l2;
+        sc->lfinal = lfinal;
+        sc->steps = steps;
+        sc->done = done;
+        sc->counter = 0;
     }
 }
 
@@ -493,9 +589,14 @@ int oc_run_impl(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, cons
     const unsigned blocks = reduce_blocks(ctx, n, 256);
     oc_init_kernel<<<blocks, 256, 0, st>>>(n, P, dc, w.partials, w.sc);
     GBS_LAUNCH_CHECK("oc_init_kernel");
-    for (int k = 0; k < prm->max_bisect; ++k) {
-        oc_step_kernel<<<blocks, 256, 0, st>>>(n, P, x, dc, preserved, w.w, w.partials, w.sc);
-        GBS_LAUNCH_CHECK("oc_step_kernel");
+    // kOcNodes double-float partials per block fit the 4 * 4096 doubles of the workspace
+    int64_t mb = (n + kOcThreads - 1) / kOcThreads;
+    const int64_t mcap = 2LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+    mb = mb > mcap ? mcap : (mb < 1 ? 1 : mb);
+    if (mb * kOcNodes > 4 * 4096) mb = (4 * 4096) / kOcNodes;
+    for (int k = 0; k < prm->max_bisect; k += kOcLevels) {
+        oc_multi_kernel<<<(unsigned)mb, kOcThreads, 0, st>>>(n, P, x, dc, preserved, w.w, (float2 *)w.partials, w.sc);
+        GBS_LAUNCH_CHECK("oc_multi_kernel");
     }
     oc_final_kernel<<<elem_blocks(ctx, n, 256), 256, 0, st>>>(n, P, x, dc, preserved, w.sc, xnew);
     GBS_LAUNCH_CHECK("oc_final_kernel");
