@@ -33,7 +33,9 @@ namespace gbs {
 
 struct ModalGeom {
     int nx, ny, nz;
-    int nseg, seglen;  // x segments: node planes [s*seglen, min((s+1)*seglen, nx+1))
+    // x segments: segment s covers planes [s seglen + min(s, rem), + seglen + (s < rem)) of the
+    // nx + 1 node planes (nx element planes for MODE_CG)
+    int nseg, seglen, rem;
 };
 
 
@@ -225,8 +227,8 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     const int F = NE - H;         // owned nodes per plane (chunk positions [H, NE))
     const int F0 = tile * F;
     constexpr bool EDGE = MODE == MODE_CG;
-    const int xs = seg * G.seglen;
-    const int xe = min(xs + G.seglen, EDGE ? nx : nx + 1);
+    const int xs = seg * G.seglen + min(seg, G.rem);
+    const int xe = min(xs + G.seglen + (seg < G.rem ? 1 : 0), EDGE ? nx : nx + 1);
     const int own_hi = (EDGE && xe == nx) ? nx + 1 : xe;  // owned node planes [xs, own_hi)
     const int x0 = EDGE ? xs : xs - 1;                     // first element plane of the pass
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -735,14 +737,13 @@ inline ModalGeom modal_geom(int nx, int ny, int nz, int num_sms, int blocks_per_
     const int tiles = (S + F - 1) / F;
     const int planes = edge ? nx : nx + 1;
     const int target = (num_sms > 0 ? num_sms : 148) * (blocks_per_sm > 0 ? blocks_per_sm : 1);
-    // As many x segments as fit in one wave of resident CTAs (rounding down, so that the
-    // re-rounded segment count never exceeds the target).
+    // As many x segments as fit in one wave of resident CTAs, of lengths that differ by at
+    // most one plane (64 element planes in 30 segments: 4 of 3 planes and 26 of 2, rather
+    // than 22 of 3).
     int nseg = target / tiles;
     if (nseg > planes) nseg = planes;
     if (nseg < 1) nseg = 1;
-    const int seglen = (planes + nseg - 1) / nseg;
-    nseg = (planes + seglen - 1) / seglen;
-    ModalGeom g{nx, ny, nz, nseg, seglen};
+    ModalGeom g{nx, ny, nz, nseg, planes / nseg, planes % nseg};
     return g;
 }
 

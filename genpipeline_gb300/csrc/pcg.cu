@@ -625,7 +625,7 @@ static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n,
         seglen[i] = (itm.nx + 1 + nseg[i] - 1) / nseg[i];
         nseg[i] = (itm.nx + 1 + seglen[i] - 1) / seglen[i];
         FusedDesign &D = T.d[i];
-        D.G = ModalGeom{itm.nx, itm.ny, itm.nz, nseg[i], seglen[i]};
+        D.G = ModalGeom{itm.nx, itm.ny, itm.nz, nseg[i], seglen[i], 0};
         D.tiles = tiles[i];
         D.block0 = block0;
         D.nblk = tiles[i] * nseg[i];
