@@ -46,7 +46,6 @@ struct ModalGeom {
 template <int NT>
 __host__ __device__ constexpr int modal_r2() { return (8 * NT - 5) / 3; }
 __host__ __device__ constexpr int modal_rw(int R) { return 4 * ((3 * R + 6) / 4); }
-__host__ __device__ constexpr int modal_pr(int R) { return 4 * ((R + 5) / 4); }
 template <int NT>
 __host__ __device__ constexpr int modal_layout_r(int R) { return (3 * R + 6) / 4 <= 2 * NT ? modal_r2<NT>() : R; }
 
@@ -59,8 +58,8 @@ __host__ __device__ constexpr int modal_layout_r(int R) { return (3 * R + 6) / 4
 template <int NT, int EPT>
 inline size_t modal_smem_bytes(int nz, bool cg) {
     const int NE = NT * EPT, H = nz + 2, R = modal_layout_r<NT>(NE + H);
-    const size_t RW = (size_t)modal_rw(R), PR = (size_t)modal_pr(R);
-    return 12 * PR * sizeof(float) + (cg ? 6 : 1) * RW * sizeof(float) + (2 + 6) * (size_t)NT * sizeof(float2) +
+    const size_t RW = (size_t)modal_rw(R);
+    return 4 * RW * sizeof(float) + (cg ? 6 : 1) * RW * sizeof(float) + (2 + 6) * (size_t)NT * sizeof(float2) +
            2 * (size_t)(NT / 32) * 6 * sizeof(float2);
 }
 
@@ -237,13 +236,12 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     const int RW = modal_rw(RL);
     const int64_t NW = 3LL * (nx + 1) * S;  // words of a node vector
 
-    const int PR = modal_pr(RL);                // floats per component row (>= R + 2)
     // One barrier per plane step: the operand planes are a ring of four slots and the y-slots
     // and warp-boundary terms alternate by step parity, so that a step's writes never meet
     // the previous step's reads of the same buffer (a slot is rewritten two barriers after
     // its last read).
-    float *Pn = smem;                           // [4][3][PR] operand planes by component; node l at 1 + l
-    float *Raw = Pn + 12 * PR;                  // [NR][RW] cp.async buffers
+    float *Pn = smem;                           // [4][RW] operand planes in the staged word order
+    float *Raw = Pn + 4 * RW;                   // [NR][RW] cp.async buffers
     float2 *Es2 = (float2 *)(Raw + NR * RW);    // [2][NT] element moduli (tid, tid + NT)
     float2 *Z1s = Es2 + 2 * NT;                 // [2][3][NT] y+1-side contributions (c) per element
     float2 *Bd = Z1s + 6 * NT;                  // [2][NT/32][6] z+1-side contributions (cy, c) of lane 31
@@ -262,6 +260,10 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
         int64_t A;
         int pad, nv, lo3, hi3, olo3, ohi3;
         bool pv, own;
+    };
+    // W0 mod 4 of node plane j (the PlaneW pad), in unsigned arithmetic (wraps mod 2^32)
+    auto plane_pad = [&](int j) -> int {
+        return (int)((3u * ((unsigned)j * (unsigned)S + (unsigned)(F0 - H))) & 3u);
     };
     auto plane_w = [&](int j) {
         PlaneW P;
@@ -306,7 +308,7 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     auto commit_plane = [&](int slot, int j) {
         const PlaneW P = plane_w(j);
         cp_async_wait_all();
-        float *Pf = Pn + slot * 3 * PR + 1;  // component c of chunk node l at Pf[c PR + l]
+        float *Pf = Pn + slot * RW;  // group f at Pf[4f]: component c of chunk node l at Pf[pad + 3 l + c]
 #pragma unroll
         for (int q = 0; q < MAXV; ++q) {
             const int f = tid + q * NT;
@@ -389,18 +391,7 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                         }
                     }
                 }
-                // scatter into the component rows: chunk word cw = 3 l + c -> Pf[c PR + l]
-                // (cw0 >= -3, so l >= -1; l <= R; both ends are spare slots)
-                int l = (cw0 + 3) / 3 - 1;
-                int c = cw0 - 3 * l;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    Pf[c * PR + l] = val[k];
-                    if (++c == 3) {
-                        c = 0;
-                        ++l;
-                    }
-                }
+                *(float4 *)(Pf + 4 * f) = make_float4(val[0], val[1], val[2], val[3]);
             }
         }
     };
@@ -495,6 +486,8 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     for (int i = x0; i <= xlast; ++i) {  // modal_geom makes every segment non-empty
         const int k = i - x0;
         const int s0 = k & 3, s1 = (k + 1) & 3, s2 = (k + 2) & 3;
+        // component c of chunk node l: plane i at P0[3 l + c], plane i + 1 at P1[3 l + c]
+        const float *P0 = Pn + s0 * RW + plane_pad(i), *P1 = Pn + s1 * RW + plane_pad(i + 1);
         float2 *Z1k = Z1s + (k & 1) * 3 * NT, *Bdk = Bd + (k & 1) * (NT / 32) * 6;
         const int es = k & 1;
         const bool more_nodes = i + 2 <= xe;
@@ -521,9 +514,9 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
 #pragma unroll
             for (int b = 0; b < 8; ++b) {
                 const int cx = b >> 2, cy = (b >> 1) & 1, cz = b & 1;
-                const float *src = Pn + (cx ? s1 : s0) * 3 * PR + 1 + tid + cy * NZ + cz;
+                const float *src = (cx ? P1 : P0) + 3 * (tid + cy * NZ + cz);
 #pragma unroll
-                for (int c = 0; c < 3; ++c) v[b][c] = make_float2(src[c * PR], src[c * PR + NT]);
+                for (int c = 0; c < 3; ++c) v[b][c] = make_float2(src[c], src[c + 3 * NT]);
             }
             modal_element2<true>(v, E, km);
 #pragma unroll
@@ -563,7 +556,7 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
         __syncthreads();
 
         // ---- nodes of plane i: node l = element l of this thread, stored straight to y -----
-        const float *Pu = Pn + s0 * 3 * PR + 1;
+        const float *Pu = P0;
         const float *Z1f = (const float *)Z1k, *Bdf = (const float *)Bdk;
 #pragma unroll
         for (int q = 0; q < EPT; ++q) {
@@ -572,7 +565,7 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
             if (l >= H && out_plane && flat < S) {
                 const int m = l - NZ;  // element whose y+1 corners touch node l (m >= 1)
                 const int mi = m >= NT ? 2 * (m - NT) + 1 : 2 * m;
-                const float uc[3] = {Pu[l], Pu[PR + l], Pu[2 * PR + l]};
+                const float uc[3] = {Pu[3 * l], Pu[3 * l + 1], Pu[3 * l + 2]};
                 float *yo = y + 3 * ((int64_t)i * S + flat);
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
