@@ -72,6 +72,44 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// Bulk copies (sm_90+): one thread moves a contiguous range global -> shared (16-byte aligned
+// addresses, size a multiple of 16); an mbarrier counts the bytes that have landed.
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+// The issuing thread's arrival, announcing the bytes its copies will deliver in this phase.
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+// Orders this thread's earlier shared-memory accesses before later bulk copies into them.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Waits for phase `parity` of the barrier to complete, at most kBulkWaitTries polls (each
+// poll suspends for a hardware-defined time); false when the limit ran out.
+constexpr unsigned kBulkWaitTries = 1u << 22;
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+    for (unsigned t = 0; t < kBulkWaitTries; ++t)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
 __device__ __forceinline__ float2 shfl_up2(float2 v) {
     return make_float2(__shfl_up_sync(0xffffffffu, v.x, 1), __shfl_up_sync(0xffffffffu, v.y, 1));
 }
@@ -180,7 +218,8 @@ struct CgPass {
     float alpha, beta;
     const float *r, *w, *sold, *dinv;
     float *rnew, *snew, *p, *xu;
-    float *clear;  // MODE_CG: the next launch's output w (its shared node planes are zeroed here)
+    float *clear;     // MODE_CG: the next launch's output w (its shared node planes are zeroed here)
+    PcgScalars *sc;   // MODE_CG: where a copy wait that ran out records GBS_ETIMEOUT
 };
 
 template <int MODE>
@@ -281,8 +320,69 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     };
 
     // ---- staging ---------------------------------------------------------------------------
+    // MODE_CG stages with bulk copies: thread 0 copies the plane's whole 16-byte groups of r, w,
+    // s and 1/diag and the owned groups of p and x (one copy per vector), and an mbarrier phase
+    // per plane counts the bytes. Only a group cut by the end of the vectors is copied by its
+    // thread with cp.async (zero-filled). The raw buffers are rewritten only after a block
+    // barrier that follows every thread's reads of the previous plane.
+    constexpr bool BULK = MODE == MODE_CG;
+    __shared__ unsigned long long s_bar;
+    unsigned bphase = 0;  // phase of the plane being committed
+    bool bulk_ok = true;  // false once a wait ran out (then no further waits)
+    if (BULK) {
+        if (tid == 0) mbar_init(&s_bar, 1);
+        __syncthreads();
+    }
+    auto bulk_wait = [&]() {
+        if (bulk_ok && !mbar_wait(&s_bar, bphase)) {
+            bulk_ok = false;
+            atomicExch(&cp.sc->status, (int)GBS_ETIMEOUT);
+            atomicExch(&cp.sc->done, 1);
+        }
+        bphase ^= 1u;
+    };
     auto issue_plane = [&](int j) {
         const PlaneW P = plane_w(j);
+        if (BULK) {
+            const int64_t full = NW & ~(int64_t)3;  // words in whole groups
+            if (tid == 0) {
+                unsigned nfull = 0, nown = 0;
+                int64_t g0 = 0, o0 = 0;
+                if (P.pv) {
+                    g0 = max(P.A, (int64_t)0);
+                    const int64_t g1 = min(P.A + 4 * (int64_t)P.nv, full);
+                    if (g1 > g0) nfull = (unsigned)(g1 - g0);
+                    if (P.own) {  // groups that meet the owned words [olo3, ohi3)
+                        o0 = max(P.A + 4 * (int64_t)((P.olo3 + P.pad) >> 2), (int64_t)0);
+                        const int64_t o1 = min(P.A + 4 * (int64_t)((P.ohi3 + P.pad + 3) >> 2), full);
+                        if (o1 > o0) nown = (unsigned)(o1 - o0);
+                    }
+                }
+                mbar_arrive_expect_tx(&s_bar, 4u * (4u * nfull + 2u * nown));
+                fence_proxy_async();
+                if (nfull)
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+                        bulk_copy_g2s(Raw + a * RW + (g0 - P.A), src_of(a) + g0, 4u * nfull, &s_bar);
+                if (nown)
+#pragma unroll
+                    for (int a = 4; a < 6; ++a)
+                        bulk_copy_g2s(Raw + a * RW + (o0 - P.A), src_of(a) + o0, 4u * nown, &s_bar);
+            }
+            if (P.pv && full < NW && full >= P.A) {  // the group cut by the end of the vectors
+                const int64_t ft = (full - P.A) >> 2;
+                if (ft < P.nv && (int)(ft % NT) == tid) {
+                    const int f = (int)ft, cw0 = 4 * f - P.pad;
+                    const int nb = 4 * (int)(NW - full);
+                    const bool ownable = P.own && cw0 + 4 > P.olo3 && cw0 < P.ohi3;
+#pragma unroll
+                    for (int a = 0; a < NR; ++a)
+                        if (a < 4 || ownable) cp_async16(Raw + a * RW + 4 * f, src_of(a) + full, nb);
+                }
+            }
+            cp_async_commit();
+            return;
+        }
 #pragma unroll
         for (int q = 0; q < MAXV; ++q) {
             const int f = tid + q * NT;
@@ -308,6 +408,7 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     auto commit_plane = [&](int slot, int j) {
         const PlaneW P = plane_w(j);
         cp_async_wait_all();
+        if (BULK) bulk_wait();
         float *Pf = Pn + slot * RW;  // group f at Pf[4f]: component c of chunk node l at Pf[pad + 3 l + c]
 #pragma unroll
         for (int q = 0; q < MAXV; ++q) {
@@ -463,9 +564,11 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     issue_eplane(x0);
     if (!pre(alpha, beta)) {
         cp_async_wait_all();  // no copy may land after the CTA has left
+        if (BULK) bulk_wait();
         return false;
     }
     commit_plane(0, x0);
+    if (BULK) __syncthreads();  // every thread's reads of the raw buffers before they are refilled
     issue_plane(x0 + 1);
     commit_eplane(0);
     commit_plane(1, x0 + 1);
@@ -668,7 +771,7 @@ __global__ void __launch_bounds__(NT, 2)
     const int nblk = gridDim.x * gridDim.y;
     const int bid = blockIdx.x + gridDim.x * blockIdx.y;
     const int par = phase & 1;
-    CgPass cp{0.0f, 0.0f, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    CgPass cp{0.0f, 0.0f, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     if (MODE == MODE_CG) {
         // Launch k runs iteration k while the solve lasts, so the vector parity is the launch
         // parity (and w cycles with k mod 3): the first plane's copies go out before the state
@@ -681,7 +784,7 @@ __global__ void __launch_bounds__(NT, 2)
         float *w_c = w3 == 0 ? ca.w[0] : w3 == 1 ? ca.w[1] : ca.w[2];
         float *w_n = w3 == 0 ? ca.w[1] : w3 == 1 ? ca.w[2] : ca.w[0];
         float *w_z = w3 == 0 ? ca.w[2] : w3 == 1 ? ca.w[0] : ca.w[1];
-        cp = CgPass{0.0f, 0.0f, r_c, w_c, s_n, ca.dinv, r_n, s_c, ca.p, ca.xu, w_z};
+        cp = CgPass{0.0f, 0.0f, r_c, w_c, s_n, ca.dinv, r_n, s_c, ca.p, ca.xu, w_z, ca.sc};
         y = w_n;
     }
     auto pre = [&](float &alpha, float &beta) -> bool {
