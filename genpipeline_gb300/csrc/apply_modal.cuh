@@ -320,30 +320,30 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     };
 
     // ---- staging ---------------------------------------------------------------------------
-    // MODE_CG stages with bulk copies: thread 0 copies the plane's whole 16-byte groups of r, w,
-    // s and 1/diag and the owned groups of p and x (one copy per vector), and an mbarrier phase
-    // per plane counts the bytes. Only a group cut by the end of the vectors is copied by its
-    // thread with cp.async (zero-filled). The raw buffers are rewritten only after a block
-    // barrier that follows every thread's reads of the previous plane.
-    constexpr bool BULK = MODE == MODE_CG;
+    // Bulk copies: thread 0 copies the plane's whole 16-byte groups of p (plain apply) or of r,
+    // w, s and 1/diag, and the owned groups of p and x (PCG modes), one copy per vector, and an
+    // mbarrier phase per plane counts the bytes. Only a group cut by the end of the vectors is
+    // copied by its thread with cp.async (zero-filled). The raw buffers are rewritten only after
+    // a block barrier that follows every thread's reads of the previous plane.
+    constexpr int NF = CG ? 4 : 1;  // vectors staged over the whole plane
     __shared__ unsigned long long s_bar;
     unsigned bphase = 0;  // phase of the plane being committed
     bool bulk_ok = true;  // false once a wait ran out (then no further waits)
-    if (BULK) {
-        if (tid == 0) mbar_init(&s_bar, 1);
-        __syncthreads();
-    }
+    if (tid == 0) mbar_init(&s_bar, 1);
+    __syncthreads();
     auto bulk_wait = [&]() {
         if (bulk_ok && !mbar_wait(&s_bar, bphase)) {
             bulk_ok = false;
-            atomicExch(&cp.sc->status, (int)GBS_ETIMEOUT);
-            atomicExch(&cp.sc->done, 1);
+            if (cp.sc) {
+                atomicExch(&cp.sc->status, (int)GBS_ETIMEOUT);
+                atomicExch(&cp.sc->done, 1);
+            }
         }
         bphase ^= 1u;
     };
     auto issue_plane = [&](int j) {
         const PlaneW P = plane_w(j);
-        if (BULK) {
+        {
             const int64_t full = NW & ~(int64_t)3;  // words in whole groups
             if (tid == 0) {
                 unsigned nfull = 0, nown = 0;
@@ -352,19 +352,19 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                     g0 = max(P.A, (int64_t)0);
                     const int64_t g1 = min(P.A + 4 * (int64_t)P.nv, full);
                     if (g1 > g0) nfull = (unsigned)(g1 - g0);
-                    if (P.own) {  // groups that meet the owned words [olo3, ohi3)
+                    if (CG && P.own) {  // groups that meet the owned words [olo3, ohi3)
                         o0 = max(P.A + 4 * (int64_t)((P.olo3 + P.pad) >> 2), (int64_t)0);
                         const int64_t o1 = min(P.A + 4 * (int64_t)((P.ohi3 + P.pad + 3) >> 2), full);
                         if (o1 > o0) nown = (unsigned)(o1 - o0);
                     }
                 }
-                mbar_arrive_expect_tx(&s_bar, 4u * (4u * nfull + 2u * nown));
+                mbar_arrive_expect_tx(&s_bar, 4u * (NF * nfull + 2u * nown));
                 fence_proxy_async();
                 if (nfull)
 #pragma unroll
-                    for (int a = 0; a < 4; ++a)
+                    for (int a = 0; a < NF; ++a)
                         bulk_copy_g2s(Raw + a * RW + (g0 - P.A), src_of(a) + g0, 4u * nfull, &s_bar);
-                if (nown)
+                if (CG && nown)
 #pragma unroll
                     for (int a = 4; a < 6; ++a)
                         bulk_copy_g2s(Raw + a * RW + (o0 - P.A), src_of(a) + o0, 4u * nown, &s_bar);
@@ -377,38 +377,19 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                     const bool ownable = P.own && cw0 + 4 > P.olo3 && cw0 < P.ohi3;
 #pragma unroll
                     for (int a = 0; a < NR; ++a)
-                        if (a < 4 || ownable) cp_async16(Raw + a * RW + 4 * f, src_of(a) + full, nb);
+                        if (a < NF || ownable) cp_async16(Raw + a * RW + 4 * f, src_of(a) + full, nb);
                 }
             }
             cp_async_commit();
-            return;
         }
-#pragma unroll
-        for (int q = 0; q < MAXV; ++q) {
-            const int f = tid + q * NT;
-            if (f < P.nv) {
-                const int cw0 = 4 * f - P.pad;
-                const int64_t gw = P.A + 4 * (int64_t)f;
-                int nb = 0;  // bytes of the group inside the vector, when it meets the plane's nodes
-                if (P.pv && cw0 + 4 > P.lo3 && cw0 < P.hi3 && gw >= 0 && gw < NW)
-                    nb = 4 * (int)(NW - gw < 4 ? NW - gw : 4);
-                const bool ownable = P.own && cw0 + 4 > P.olo3 && cw0 < P.ohi3;
-#pragma unroll
-                for (int a = 0; a < NR; ++a) {
-                    const bool need = a < 4 || ownable;  // p and x only where nodes are owned
-                    if (nb > 0 && need) cp_async16(Raw + a * RW + 4 * f, src_of(a) + gw, nb);
-                }
-            }
-        }
-        cp_async_commit();
     };
-    // Combines the staged groups of plane j (this thread's own copies) into operand slot
+    // Combines the staged groups of plane j into operand slot
     // `slot`; in the PCG modes also updates s, r, p and x of the owned words. Interior groups
     // (all four words inside the plane, and all or none owned) take a branch-free path.
     auto commit_plane = [&](int slot, int j) {
         const PlaneW P = plane_w(j);
         cp_async_wait_all();
-        if (BULK) bulk_wait();
+        bulk_wait();
         float *Pf = Pn + slot * RW;  // group f at Pf[4f]: component c of chunk node l at Pf[pad + 3 l + c]
 #pragma unroll
         for (int q = 0; q < MAXV; ++q) {
@@ -564,11 +545,11 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     issue_eplane(x0);
     if (!pre(alpha, beta)) {
         cp_async_wait_all();  // no copy may land after the CTA has left
-        if (BULK) bulk_wait();
+        bulk_wait();
         return false;
     }
     commit_plane(0, x0);
-    if (BULK) __syncthreads();  // every thread's reads of the raw buffers before they are refilled
+    __syncthreads();  // every thread's reads of the raw buffers before they are refilled
     issue_plane(x0 + 1);
     commit_eplane(0);
     commit_plane(1, x0 + 1);

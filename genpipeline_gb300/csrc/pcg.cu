@@ -513,7 +513,7 @@ __global__ void __launch_bounds__(NT, 2)
     unsigned target = 0;
     while (!done) {
         const int c = it & 1, nc = c ^ 1;
-        const CgPass cp{alpha.hi, beta.hi, ca.r[c], ca.w[c], ca.s[nc], ca.dinv, ca.r[nc], ca.s[c], ca.p, ca.xu, nullptr, nullptr};
+        const CgPass cp{alpha.hi, beta.hi, ca.r[c], ca.w[c], ca.s[nc], ca.dinv, ca.r[nc], ca.s[c], ca.p, ca.xu, nullptr, ca.sc};
         float sums[3];
         modal_pass<NT, EPT, MAXV, MODE_CG_FUSED>(G, D.x, nullptr, ca.w[nc], D.mask, law, km, cp, (float *)smem4, tile, seg,
                                                  sums, [](float &, float &) { return true; });
