@@ -308,8 +308,6 @@ __device__ __forceinline__ float oc_trial(float x, float dc, float inv_l, const 
 
 __global__ void oc_init_kernel(int64_t n, const OcParams P, const float *__restrict__ dc, double *partials,
                                OcScalars *sc) {
-    __shared__ double sred[32];
-    __shared__ double tot[1];
     sc->done = 0;  // every block writes the same values
     sc->steps = 0;
     if (P.l2 >= 0.0) {
@@ -339,8 +337,6 @@ __global__ void oc_init_kernel(int64_t n, const OcParams P, const float *__restr
         last = (atomicAdd(&sc->counter, 1u) == gridDim.x - 1);
     }
     __syncthreads();
-    (void)sred;
-    (void)tot;
     if (last && threadIdx.x == 0) {
         __threadfence();
         double mm = -INFINITY;
