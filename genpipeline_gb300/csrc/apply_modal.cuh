@@ -15,16 +15,18 @@
 //
 // Data movement: a CTA owns F consecutive nodes of the flattened (y,z) node plane
 // (flat = j*(nz+1) + k) and walks along x. A plane's R = F + 2(nz+2) staged nodes are one
-// contiguous run of 3R words in every node vector, so each staged vector is copied as
-// 16-byte groups with cp.async (no registers held while the copies fly) into a raw buffer,
-// and combined group by group (float4) into the operand plane, laid out as one row per
-// component, so that the element pair of a thread (tid, tid + NT) loads each corner value
-// straight into the two lanes of a packed FP32x2 register. Per step the CTA computes one plane of elements from two
-// operand planes while the copies of the plane after next are in flight. Each element's 24
-// corner contributions are combined along z with a warp shuffle (the element to the left
-// is the lane to the left), along y through a 6-float shared slot per element, and along x
-// in registers (the x+1 corners are carried to the next plane): one writer per node and DOF,
-// fixed summation order, no atomics. The owned nodes' results go out as float4 groups.
+// contiguous run of 3R words in every node vector, so one thread stages each vector's run
+// with one bulk copy (cp.async.bulk, completion counted on an mbarrier) into a raw buffer,
+// and every thread combines its 16-byte groups into the operand plane, kept in the staged
+// word order, from which the element pair of a thread (tid, tid + NT) loads each corner
+// value straight into the two lanes of a packed FP32x2 register. Per step the CTA computes
+// one plane of elements from two operand planes while the copies of the plane after next
+// are in flight. Each element's 24 corner contributions are combined along z with a warp
+// shuffle (the element to the left is the lane to the left), along y through a 6-float
+// shared slot per element, and along x in registers (the x+1 corners are carried to the
+// next plane): one writer per node and DOF and a fixed summation order, except on the node
+// planes that two x segments share in the one-kernel PCG, where the two halves are added
+// onto zero (the same result in either order).
 #pragma once
 
 #include "apply_tile.cuh"
@@ -50,11 +52,10 @@ template <int NT>
 __host__ __device__ constexpr int modal_layout_r(int R) { return (3 * R + 6) / 4 <= 2 * NT ? modal_r2<NT>() : R; }
 
 // Shared memory of the modal kernel for a given z extent (NT = 256, EPT = 2): four operand
-// planes of three component rows of modal_pr floats (>= R + 2), the raw cp.async buffers of
-// modal_rw floats (one per staged vector: p for the plain apply; r, w, s, 1/diag, p, x for the
-// PCG modes), two planes of element moduli, and two copies (by step parity) of the y-direction
-// slots (3 floats per element) and of the warp-boundary contributions (6 floats per warp and
-// lane).
+// planes and the raw bulk-copy buffers (one per staged vector: p for the plain apply; r, w,
+// s, 1/diag, p, x for the PCG modes), modal_rw floats each, two planes of element moduli, and
+// two copies (by step parity) of the y-direction slots (3 floats per element) and of the
+// warp-boundary contributions (6 floats per warp and lane).
 template <int NT, int EPT>
 inline size_t modal_smem_bytes(int nz, bool cg) {
     const int NE = NT * EPT, H = nz + 2, R = modal_layout_r<NT>(NE + H);
@@ -280,7 +281,7 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     // the previous step's reads of the same buffer (a slot is rewritten two barriers after
     // its last read).
     float *Pn = smem;                           // [4][RW] operand planes in the staged word order
-    float *Raw = Pn + 4 * RW;                   // [NR][RW] cp.async buffers
+    float *Raw = Pn + 4 * RW;                   // [NR][RW] bulk-copy buffers
     float2 *Es2 = (float2 *)(Raw + NR * RW);    // [2][NT] element moduli (tid, tid + NT)
     float2 *Z1s = Es2 + 2 * NT;                 // [2][3][NT] y+1-side contributions (c) per element
     float2 *Bd = Z1s + 6 * NT;                  // [2][NT/32][6] z+1-side contributions (cy, c) of lane 31
