@@ -805,21 +805,35 @@ static int loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<f
     return GBS_OK;
 }
 
+// pcg_setup flags: the caller's start vector u is zero (q = 0, no apply), and the 1/diag in
+// the workspace is already that of this x and mask (an earlier round of the same solve).
+enum { SETUP_X0_ZERO = 1, SETUP_KEEP_DINV = 2 };
+
 // PCG setup on the stream: zeroed scalars, 1/diag, q = D K D u, r = D b - q, then for the
 // single-reduction form u_0 = M r_0, w_0 = D K D u_0 and alpha_0, for the dense form
 // p_{-1} = 0; the first dot products and the stop test (nothing is read back).
 static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x,
                      const float *b, const uint8_t *mask, float *u, double rtol, int max_iter, const PcgWs &w,
-                     cudaStream_t st) {
+                     cudaStream_t st, unsigned flags = 0) {
     const int64_t nd = n_dof_of(nx, ny, nz);
     const Law<float> law = make_law<float>(*glaw);
     GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
-    dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, law, ctx->kef, x, mask, w.dinv);
-    GBS_LAUNCH_CHECK("dinv_kernel");
+    if (!(flags & SETUP_KEEP_DINV)) {
+        dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, law, ctx->kef, x, mask, w.dinv);
+        GBS_LAUNCH_CHECK("dinv_kernel");
+    }
     const int max_trips = (max_iter + kLoopUnroll - 1) / kLoopUnroll + 2;
+    // q = D K D u into `qbuf`, or zeros when u is known to be zero
+    auto start_q = [&](float *qbuf) -> int {
+        if (flags & SETUP_X0_ZERO) {
+            GBS_CUDA_TRY(cudaMemsetAsync(qbuf, 0, (size_t)nd * sizeof(float), st));
+            return GBS_OK;
+        }
+        return apply_f32(ctx, nx, ny, nz, glaw, x, u, qbuf, mask, st);
+    };
     if (use_modal(ctx, nz)) {
         const CgArgs ca = cg_args(w, u);
-        int rc = apply_f32(ctx, nx, ny, nz, glaw, x, u, ca.w[1], mask, st);
+        int rc = start_q(ca.w[1]);
         if (rc) return rc;
         cg_init_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, b, ca.w[1], mask, w.dinv, ca.r[0], ca.p, ca.s[1], u,
                                                            w.partials, w.sc, rtol, max_iter, max_trips);
@@ -830,7 +844,7 @@ static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp
         GBS_LAUNCH_CHECK("cg_start_kernel");
         return GBS_OK;
     }
-    int rc = apply_f32(ctx, nx, ny, nz, glaw, x, u, w.ap, mask, st);
+    int rc = start_q(w.ap);
     if (rc) return rc;
     pcg_init_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, b, w.ap, mask, w.dinv, w.r, w.p1, u, w.partials, w.sc, rtol,
                                                         max_iter, max_trips);
@@ -850,11 +864,11 @@ struct ApplyProfile {
 // together with its own.
 int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x, const float *b,
             const uint8_t *mask, float *u, double rtol, int max_iter, int check_every, void *ws, PcgScalars *out,
-            cudaStream_t st, ApplyProfile *prof = nullptr, int fused = 0) {
+            cudaStream_t st, ApplyProfile *prof = nullptr, int fused = 0, unsigned setup_flags = 0) {
     const int64_t nd = n_dof_of(nx, ny, nz);
     PcgWs w = pcg_ws(ws, nx, ny, nz);
     const Law<float> law = make_law<float>(*glaw);
-    int rc = pcg_setup(ctx, nx, ny, nz, glaw, x, b, mask, u, rtol, max_iter, w, st);
+    int rc = pcg_setup(ctx, nx, ny, nz, glaw, x, b, mask, u, rtol, max_iter, w, st, setup_flags);
     if (rc) return rc;
     PcgScalars h;
     memset(&h, 0, sizeof h);
@@ -1096,8 +1110,10 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
         // Inner tolerance: enough to reach rtol from here, but not below what FP32 resolves.
         double itol = o->rtol / relres;
         if (itol < inner) itol = inner;
+        // d32 was zeroed above; the first round computes 1/diag, later rounds reuse it
         rc = pcg_run(ctx, nx, ny, nz, law, x, w.b32, mask, w.d32, itol, o->max_iter - total, o->check_every, w.pcg,
-                     async ? nullptr : &ps, st, o->profile ? &prof : nullptr, o->fused);
+                     async ? nullptr : &ps, st, o->profile ? &prof : nullptr, o->fused,
+                     SETUP_X0_ZERO | (outer > 1 ? SETUP_KEEP_DINV : 0u));
         if (rc) return rc;
         if (async) {
             pending = pw.sc;
@@ -1562,7 +1578,7 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
         if (itol < inner) itol = inner;
         PcgWs pw = pcg_ws(w.pcg, it.nx, it.ny, it.nz);
         int rc = pcg_setup(ctx, it.nx, it.ny, it.nz, glaw, it.x, w.b32, it.node_mask, w.d32, itol,
-                           o->max_iter - it.stats.iterations, pw, st);
+                           o->max_iter - it.stats.iterations, pw, st, SETUP_X0_ZERO);
         if (rc) return rc;
     }
     // persistent batched launches (fall back to each item's graph loop)
