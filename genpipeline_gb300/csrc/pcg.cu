@@ -239,10 +239,9 @@ __global__ void cg_init_kernel(int64_t nd, const float *__restrict__ b, float *q
 }
 
 // Single-reduction setup, step 2 (after w_0 = D K D u_0): alpha_0 = (r_0.u_0) / (w_0.u_0),
-// beta_0 = 0. u_0 (in w[1], no longer needed) is cleared as it is read: the first launch adds
-// its output into w[1] on the segments' shared node planes.
-__global__ void cg_start_kernel(int64_t nd, const float *__restrict__ w, float *__restrict__ u, double *partials,
-                                PcgScalars *sc) {
+// beta_0 = 0.
+__global__ void cg_start_kernel(int64_t nd, const float *__restrict__ w, const float *__restrict__ u,
+                                double *partials, PcgScalars *sc) {
     if (sc->done) {  // the first launch reads state slot 1
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             CgState s = {};
@@ -255,10 +254,8 @@ __global__ void cg_start_kernel(int64_t nd, const float *__restrict__ w, float *
         return;
     }
     float wu = 0.0f;
-    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x)
         wu = fmaf(w[d], u[d], wu);
-        u[d] = 0.0f;
-    }
     __shared__ double tot[3];
     if (last_block3(wu, 0.0, 0.0, partials, &sc->counter, tot) && threadIdx.x == 0) {
         sc->pap = tot[0];
@@ -842,6 +839,9 @@ static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp
         if (rc) return rc;
         cg_start_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, ca.w[0], ca.w[1], w.partials, w.sc);
         GBS_LAUNCH_CHECK("cg_start_kernel");
+        // u_0 in w[1] is no longer needed: the first launch adds its output into w[1] on the
+        // segments' shared node planes, so w[1] starts at zero
+        GBS_CUDA_TRY(cudaMemsetAsync(ca.w[1], 0, (size_t)nd * sizeof(float), st));
         return GBS_OK;
     }
     int rc = start_q(w.ap);
