@@ -650,7 +650,7 @@ static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n,
 // kernels return at once when done is set, so a finished solve costs at most kLoopUnroll-1
 // empty iterations. The condition kernel also counts trips and stops
 // the loop with GBS_ETIMEOUT after max_trips (set from max_iter), so the loop always ends.
-constexpr int kLoopUnroll = 6;
+constexpr int kLoopUnroll = 12;
 static_assert(kLoopUnroll % 6 == 0, "a trip must end on launch phase 5 (parity 1, w index 2)");
 
 static inline int launches_per_trip(const gbsimp_ctx *ctx, int nz) {
