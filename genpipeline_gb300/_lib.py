@@ -73,6 +73,11 @@ class BatchItem(C.Structure):
                 ("ws", C.c_void_p), ("ws_bytes", C.c_size_t), ("stats", SolveStats)]
 
 
+class SimpOpts(C.Structure):
+    _fields_ = [("volfrac", C.c_double), ("rmin", C.c_double), ("n_iters", C.c_int32), ("early_stop", C.c_int32),
+                ("oc", OcParams), ("solve", SolveOpts)]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _I64 = C.c_int64
@@ -113,6 +118,14 @@ SIGNATURES = {
                           C.POINTER(SolveStats), _P, _SZ, _P]),
     "gbsimp_batch_round": (_I, [_P, C.POINTER(BatchItem), _I, C.POINTER(Law), C.POINTER(SolveOpts), _P]),
     "gbsimp_batch_solve": (_I, [_P, C.POINTER(BatchItem), _I, C.POINTER(Law), C.POINTER(SolveOpts), _P]),
+    "gbsimp_queue_create": (_I, [_P, C.POINTER(Law), C.POINTER(SolveOpts), C.POINTER(_P)]),
+    "gbsimp_queue_destroy": (_I, [_P]),
+    "gbsimp_queue_submit": (_I, [_P, C.POINTER(BatchItem)]),
+    "gbsimp_queue_poll": (_I, [_P, C.POINTER(C.POINTER(BatchItem)), _I, C.POINTER(C.c_int), _P]),
+    "gbsimp_queue_size": (_I, [_P]),
+    "gbsimp_simp_run_ws_bytes": (_SZ, [_I, _I, _I]),
+    "gbsimp_simp_run": (_I, [_P, _I, _I, _I, C.POINTER(Law), C.POINTER(SimpOpts), _P, _P, _P, _P, _P, _P,
+                             C.POINTER(_D), C.POINTER(C.c_int32), C.POINTER(SolveStats), _P, _SZ, _P]),
     "gbsimp_pcg_csr_ws_bytes": (_SZ, [_I64]),
     "gbsimp_pcg_csr_f32": (_I, [_P, _I64, _P, _P, _P, _P, _P, _P, _P, _I64, C.POINTER(SolveOpts),
                                 C.POINTER(SolveStats), _P, _SZ, _P]),

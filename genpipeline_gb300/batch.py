@@ -115,6 +115,61 @@ class BatchFEM:
         return out
 
 
+class SolveQueue:
+    """The native solve queue (gbsimp_queue_*): designs are submitted at any time, each poll
+    runs one defect-correction round for everything queued (the persistent batched PCG
+    inside) and hands back the designs that finished. The same continuous batching as
+    BatchFEM, with the queue kept by the library."""
+
+    def __init__(self, engine: Optional[Engine] = None, law: Optional[L.Law] = None, rtol: float = 1e-8,
+                 inner_rtol: float = 1e-4, max_iter: int = 200000, max_outer: int = 30, fused: bool = True):
+        self.eng = engine or get_engine()
+        self.law = law or L.make_law("modified", 3.0)
+        self.opts = Engine.opts(rtol=rtol, inner_rtol=inner_rtol, max_iter=max_iter, max_outer=max_outer,
+                                fused=int(fused))
+        h = C.c_void_p()
+        L.check(self.eng.lib.gbsimp_queue_create(self.eng.ctx, C.byref(self.law), C.byref(self.opts), C.byref(h)))
+        self._q = h
+        self._by_addr = {}  # address of a submitted item struct -> its design (keeps the struct alive)
+        self._uploader = BatchFEM(self.eng, self.law)
+
+    def submit(self, d: FEMDesign) -> FEMDesign:
+        if d.dx is None:
+            self._uploader.upload(d)
+        d._qitem = L.BatchItem(d.grid[0], d.grid[1], d.grid[2], 0, d.dx.data_ptr(), d.df.data_ptr(),
+                               d.dmask.data_ptr(), d.du.data_ptr(), d.ws.data_ptr(), d.ws.numel(), L.SolveStats())
+        L.check(self.eng.lib.gbsimp_queue_submit(self._q, C.byref(d._qitem)))
+        self._by_addr[C.addressof(d._qitem)] = d
+        return d
+
+    def poll(self, max_done: int = 64) -> List[FEMDesign]:
+        arr = (C.POINTER(L.BatchItem) * max_done)()
+        n = C.c_int()
+        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        L.check(self.eng.lib.gbsimp_queue_poll(self._q, arr, max_done, C.byref(n), stream))
+        out = []
+        for k in range(n.value):
+            d = self._by_addr.pop(C.addressof(arr[k].contents))
+            d.stats = d._qitem.stats.as_dict()
+            d.compliance = float(torch.dot(d.df, d.du).item())
+            out.append(d)
+        return out
+
+    def __len__(self) -> int:
+        return int(self.eng.lib.gbsimp_queue_size(self._q))
+
+    def close(self):
+        if self._q:
+            self.eng.lib.gbsimp_queue_destroy(self._q)
+            self._q = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def solve_plain(designs: List[FEMDesign], engine: Optional[Engine] = None, law: Optional[L.Law] = None,
                 rtol: float = 1e-8, inner_rtol: float = 1e-4) -> List[FEMDesign]:
     """The one-design-at-a-time form: one gbsimp_solve (graph-loop PCG) per design."""

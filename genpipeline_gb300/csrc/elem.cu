@@ -554,6 +554,8 @@ namespace gbs {
 
 size_t oc_ws_bytes_impl(int64_t n) { return oc_ws_bytes(n); }
 
+const float *oc_ws_hs(const void *ws, int64_t n) { return oc_ws(const_cast<void *>(ws), n).hs; }
+
 int oc_prepare_impl(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const uint8_t *preserved, void *ws,
                     cudaStream_t st) {
     const int64_t n = (int64_t)nx * ny * nz;

@@ -18,6 +18,8 @@ int apply_f64_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_
                     const double *p, double *y, const uint8_t *mask, double *C, cudaStream_t st);
 // OC update with an explicit scratch pointer (layout of gbsimp_oc_ws_bytes).
 size_t oc_ws_bytes_impl(int64_t n_elem);
+// The filter row sums Hs inside an OC workspace (valid after oc_prepare_impl).
+const float *oc_ws_hs(const void *ws, int64_t n_elem);
 int oc_check_args(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_oc_params *prm, const float *x,
                   const float *dc, const float *xnew, const float *xphys);
 int oc_prepare_impl(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const uint8_t *preserved, void *ws,

@@ -258,6 +258,34 @@ class Engine:
                                       C.byref(st), _p(ws), nb, _stream()))
         return st.as_dict()
 
+    def simp_run(self, grid: Grid, law: L.Law, f: torch.Tensor, mask: Optional[torch.Tensor], x: torch.Tensor,
+                 u: torch.Tensor, volfrac: float, rmin: float, n_iters: int, preserved: Optional[torch.Tensor] = None,
+                 oc_variant=None, early_stop: bool = False, rtol=1e-8, inner_rtol=1e-4, max_iter=100000,
+                 max_outer=30, fused=False, key: str = "simp_run"):
+        """The whole SIMP loop in one native call (gbsimp_simp_run). x: initial design in, final
+        design out; u: warm start in, last displacement out. Returns (xphys, objective per
+        iteration, stats of the last solve)."""
+        nx, ny, nz = grid
+        ne, nd = n_elem(grid), n_dof(grid)
+        _need(x, torch.float32, ne, "x")
+        _need(f, torch.float64, nd, "f")
+        _need(u, torch.float64, nd, "u")
+        if preserved is not None:
+            _need(preserved, torch.uint8, ne, "preserved")
+        xphys = torch.empty_like(x)
+        so = L.SimpOpts(float(volfrac), float(rmin), int(n_iters), int(bool(early_stop)), L.make_oc(volfrac, oc_variant),
+                        self.opts(rtol=rtol, inner_rtol=inner_rtol, max_iter=max_iter, max_outer=max_outer,
+                                  fused=int(fused)))
+        nb = self.lib.gbsimp_simp_run_ws_bytes(nx, ny, nz)
+        ws = self.workspace(key, nb)
+        obj = (C.c_double * max(int(n_iters), 1))()
+        its = C.c_int32()
+        st = L.SolveStats()
+        L.check(self.lib.gbsimp_simp_run(self.ctx, nx, ny, nz, C.byref(law), C.byref(so), _p(f), _p(mask),
+                                         _p(preserved), _p(x), _p(xphys), _p(u), obj, C.byref(its), C.byref(st),
+                                         _p(ws), nb, _stream()))
+        return xphys, [float(v) for v in obj[:its.value]], st.as_dict()
+
     def pcg_csr(self, row_ptr, col_idx, values, diagonal, b, x, fixed, rtol=1e-6, max_iter=100) -> dict:
         n = b.numel()
         _need(b, torch.float32, n, "b")

@@ -245,6 +245,55 @@ int gbsimp_batch_round(gbsimp_ctx *ctx, gbsimp_batch_item *items, int n, const g
 int gbsimp_batch_solve(gbsimp_ctx *ctx, gbsimp_batch_item *items, int n, const gbsimp_law *law,
                        const gbsimp_solve_opts *opts, void *stream);
 
+/* ---- solve queue (continuous batching behind submit / poll) ---------------------------- */
+/* A queue of solves advanced together by gbsimp_batch_round (one FP64 round per poll, with
+ * the persistent batched PCG inside). Replaces the evaluator's thread pool of one solve per
+ * design (voxel_fem.py:559-611 over gpu_fem_solver.py:76-133) for a serving loop: requests
+ * join between rounds as they arrive and leave when they are done. The queue keeps pointers to
+ * the submitted items; their buffers and workspaces stay the caller's until poll returns
+ * them. All items of a queue share the law and the solve options given at creation. */
+typedef struct gbsimp_queue gbsimp_queue;
+int gbsimp_queue_create(gbsimp_ctx *ctx, const gbsimp_law *law, const gbsimp_solve_opts *opts,
+                        gbsimp_queue **out);
+int gbsimp_queue_destroy(gbsimp_queue *q);
+/* Adds an item (its state is set to 0: it joins the next round). u holds its warm start. */
+int gbsimp_queue_submit(gbsimp_queue *q, gbsimp_batch_item *item);
+/* Runs one round for every queued item, then hands back up to max_done finished items
+ * (state != 0, stats filled) in done[0..*n_done); finished items beyond max_done are handed
+ * back by the next polls. Synchronises the stream. */
+int gbsimp_queue_poll(gbsimp_queue *q, gbsimp_batch_item **done, int max_done, int *n_done,
+                      void *stream);
+/* Items queued or finished and not yet handed back. */
+int gbsimp_queue_size(const gbsimp_queue *q);
+
+/* ---- SIMP loop --------------------------------------------------------------------------- */
+typedef struct gbsimp_simp_opts {
+    double volfrac;            /* target volume fraction (replaces oc.volfrac) */
+    double rmin;               /* density filter radius */
+    int32_t n_iters;           /* OC iterations */
+    int32_t early_stop;        /* 1: stop after three consecutive relative changes below 1% of
+                                  the objective (the rule of SIMPSolverGPU.run,
+                                  simp_solver_gpu.py:111-125, which tests a fresh compliance
+                                  solve after each update; here each iteration's own objective,
+                                  so the stop comes one design later) */
+    gbsimp_oc_params oc;       /* the bisection (CPU or GPU variant parameters) */
+    gbsimp_solve_opts solve;   /* the FP64-refined solves */
+} gbsimp_simp_opts;
+/* The SIMP loop of SIMPSolver.run (simp_solver.py:56-79) in one call: xphys = x, then per
+ * iteration the solve K(xphys) u = f (u warm-starts the next), the element energies and
+ * dc = -dE/dx ce at xphys, dc <- H^T(dc / Hs), and the OC update of x (xphys = H xnew / Hs,
+ * preserved elements 1). x: initial design in, final design out; xphys: out; u: FP64 warm
+ * start in, the last solve's displacement out. compliance (host, nullable, n_iters doubles)
+ * receives sum_e E_e ce_e of each iteration (the reference's objective); reading it, and the
+ * early stop, cost one stream synchronisation per iteration. *iters_out: iterations run.
+ * *last_stats: the last solve. Stops with the solve's status on a failed solve. */
+size_t gbsimp_simp_run_ws_bytes(int nx, int ny, int nz);
+int gbsimp_simp_run(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
+                    const gbsimp_simp_opts *opts, const double *f, const uint8_t *node_mask,
+                    const uint8_t *preserved, float *x, float *xphys, double *u,
+                    double *compliance, int32_t *iters_out, gbsimp_solve_stats *last_stats,
+                    void *ws, size_t ws_bytes, void *stream);
+
 /* Jacobi-PCG on a CSR matrix (int32 row_ptr/col_idx, FP32 values, FP32 diagonal), the
  * contract of cuda_kernels.pcg_solve_cuda (cuda_kernels/__init__.py:443-473,
  * simp_pcg_cuda.cu:66-124): x holds x0 on entry; fixed is a list of n_fixed DOF indices

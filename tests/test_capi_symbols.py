@@ -59,3 +59,16 @@ def test_workspace_queries_are_host_only():
         assert lib.gbsimp_solve_ws_bytes(*grid) >= lib.gbsimp_pcg_ws_bytes(*grid) + 16 * nd
         assert lib.gbsimp_oc_ws_bytes(*grid) >= 8 * grid[0] * grid[1] * grid[2]
     assert lib.gbsimp_pcg_csr_ws_bytes(1000) >= 16000
+
+
+def test_queue_and_simp_run_argument_checks_without_gpu():
+    """Host-only paths of the queue and the SIMP loop: size queries and argument errors."""
+    lib = L.load()
+    assert lib.gbsimp_simp_run_ws_bytes(0, 4, 4) == 0
+    assert lib.gbsimp_simp_run_ws_bytes(8, 4, 4) > lib.gbsimp_solve_ws_bytes(8, 4, 4)
+    assert lib.gbsimp_queue_size(None) == -1
+    n = C.c_int(7)
+    assert lib.gbsimp_queue_poll(None, None, 0, C.byref(n), None) == L.GBS_EINVAL
+    assert lib.gbsimp_queue_submit(None, None) == L.GBS_EINVAL
+    assert lib.gbsimp_queue_create(None, None, None, None) == L.GBS_EINVAL
+    assert C.sizeof(L.SimpOpts) == 16 + 8 + C.sizeof(L.OcParams) + C.sizeof(L.SolveOpts)
