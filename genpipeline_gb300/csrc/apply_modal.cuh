@@ -440,7 +440,7 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                             po[k] = fmaf(beta, pv[k], dv[k] * rv[k]);
                             xo[k] = fmaf(alpha, po[k], xv[k]);
                             g_ru = fmaf(rno[k], val[k], g_ru);
-                            g_rr = fmaf(rno[k], rno[k], g_rr);
+                            g_rr = dv[k] != 0.0f ? fmaf(rno[k], rno[k], g_rr) : g_rr;  // free DOFs only
                         }
                         *(float4 *)(cp.snew + gw) = make_float4(so[0], so[1], so[2], so[3]);
                         *(float4 *)(cp.rnew + gw) = make_float4(rno[0], rno[1], rno[2], rno[3]);
@@ -469,7 +469,7 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                                 cp.p[gw + k] = po;
                                 cp.xu[gw + k] = fmaf(alpha, po, xv[k]);
                                 g_ru = fmaf(rno[k], val[k], g_ru);
-                                g_rr = fmaf(rno[k], rno[k], g_rr);
+                                g_rr = dv[k] != 0.0f ? fmaf(rno[k], rno[k], g_rr) : g_rr;
                             }
                         }
                     }
@@ -586,7 +586,7 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
         for (int q = 0; q < EPT; ++q) {
             const int l = tid + q * NT;
             const bool ok = out_plane && l >= H && F0 - H + l < S;
-            om[q] = (ok && mask) ? mask[(int64_t)i * S + F0 - H + l] : (uint8_t)0;
+            om[q] = (!CG && ok && mask) ? mask[(int64_t)i * S + F0 - H + l] : (uint8_t)0;
         }
 
         // ---- element plane i: elements tid and tid + NT as the two lanes of a float2 ----
@@ -658,7 +658,9 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                     const float tl = Bdf[max(bl[q], 0) + 2 * c], tm = Bdf[max(bm[q], 0) + 2 * c];
                     s += bl[q] >= 0 ? tl : 0.0f;
                     s += bm[q] >= 0 ? tm : 0.0f;
-                    const float yc = ((om[q] >> c) & 1) ? 0.0f : s;
+                    // PCG modes leave w unmasked: 1/diag = 0 keeps u, p and x at zero on fixed
+                    // DOFs whatever w holds there, and r.r skips them (the plain apply masks)
+                    const float yc = (!CG && ((om[q] >> c) & 1)) ? 0.0f : s;
                     if (CG) g_wu = fmaf(uc[c], yc, g_wu);
                     if (shared)
                         atomicAdd(yo + c, yc);
