@@ -483,9 +483,10 @@ def run_ours(a):
     # ---- roofline of the dominant kernel (the one-kernel PCG iteration) -----------------
     path = prob.eng.apply_path(GRID[2])
     if path == "modal":
-        # r_i, w_i, s_{i-1}, 1/diag, p_{i-1}, x_i and the densities in; s_i, r_{i+1}, p_i,
-        # x_{i+1}, w_{i+1} out
-        alg_bytes = 4 * (11 * nd + ne)
+        # r_i, w_i, s_{i-1}, 1/diag, p_{i-1} and the densities in; s_i, r_{i+1}, p_i, w_{i+1}
+        # out; x read and written every other iteration (two-step update): 10 words per DOF
+        # on average, the basis of one standard Jacobi-PCG iteration
+        alg_bytes = 4 * (10 * nd + ne)
         kname = "apply_modal_kernel<CG> (one single-reduction PCG iteration: s, r, u staging, w = DKDu, p, x)"
     else:
         alg_bytes = 4 * (7 * nd + ne)  # r, dinv, p_old, x_u, x in; p_new, Ap, x_u out

@@ -221,6 +221,10 @@ struct CgPass {
     float *rnew, *snew, *p, *xu;
     float *clear;     // MODE_CG: the next launch's output w (its shared node planes are zeroed here)
     PcgScalars *sc;   // MODE_CG: where a copy wait that ran out records GBS_ETIMEOUT
+    // x update: 0 none; 1 x += alpha p_i every iteration; 2 two iterations at once,
+    // x_{i+1} = x_{i-1} + (alpha_{i-1} + alpha_i beta_i) p_{i-1} + alpha_i u_i (the odd
+    // launches of the one-kernel PCG; the even ones use 0)
+    int xmode;
 };
 
 template <int MODE>
@@ -232,9 +236,9 @@ __device__ __forceinline__ float ld_vec(const float *p) {
 // One sliding-window pass of a CTA over its (flat tile, x segment): y = D K D p on the owned
 // nodes (PLAIN), or one PCG iteration with y = w_{i+1} (CG modes). sums[] receives this
 // thread's FP32 shares of r.u, w.u and r.r (CG modes). Every node vector must be 16-byte
-// aligned. pre(alpha, beta) runs once the first plane's copies are in flight (the step's
-// scalars can be formed meanwhile); when it returns false the pass stops there (returns
-// false).
+// aligned. pre(alpha, beta, alpha_prev) runs once the first plane's copies are in flight (the
+// step's scalars can be formed meanwhile); when it returns false the pass stops there
+// (returns false).
 //
 // Segments. PLAIN and CG_FUSED: segment s owns node planes [xs, xe) of nx + 1 and also
 // computes element plane xs - 1 (a halo step) so that every owned node sums all its elements.
@@ -286,7 +290,7 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     float2 *Z1s = Es2 + 2 * NT;                 // [2][3][NT] y+1-side contributions (c) per element
     float2 *Bd = Z1s + 6 * NT;                  // [2][NT/32][6] z+1-side contributions (cy, c) of lane 31
 
-    float alpha = cp.alpha, beta = cp.beta;
+    float alpha = cp.alpha, beta = cp.beta, alpha_prev = 0.0f, c1 = 0.0f;
     float g_ru = 0.0f, g_wu = 0.0f, g_rr = 0.0f;  // FP32 per-thread partials
     sums[0] = sums[1] = sums[2] = 0.0f;
 
@@ -359,7 +363,8 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                         if (o1 > o0) nown = (unsigned)(o1 - o0);
                     }
                 }
-                mbar_arrive_expect_tx(&s_bar, 4u * (NF * nfull + 2u * nown));
+                const unsigned nown_vec = cp.xmode ? 2u : 1u;  // p, and x when it is updated
+                mbar_arrive_expect_tx(&s_bar, 4u * (NF * nfull + nown_vec * nown));
                 fence_proxy_async();
                 if (nfull)
 #pragma unroll
@@ -368,7 +373,8 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                 if (CG && nown)
 #pragma unroll
                     for (int a = 4; a < 6; ++a)
-                        bulk_copy_g2s(Raw + a * RW + (o0 - P.A), src_of(a) + o0, 4u * nown, &s_bar);
+                        if (a == 4 || cp.xmode)
+                            bulk_copy_g2s(Raw + a * RW + (o0 - P.A), src_of(a) + o0, 4u * nown, &s_bar);
             }
             if (P.pv && full < NW && full >= P.A) {  // the group cut by the end of the vectors
                 const int64_t ft = (full - P.A) >> 2;
@@ -378,7 +384,8 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                     const bool ownable = P.own && cw0 + 4 > P.olo3 && cw0 < P.ohi3;
 #pragma unroll
                     for (int a = 0; a < NR; ++a)
-                        if (a < NF || ownable) cp_async16(Raw + a * RW + 4 * f, src_of(a) + full, nb);
+                        if (a < NF || (ownable && (a == 4 || cp.xmode)))
+                            cp_async16(Raw + a * RW + 4 * f, src_of(a) + full, nb);
                 }
             }
             cp_async_commit();
@@ -432,29 +439,32 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                     }
                     if (own_all) {
                         const float4 p4 = *(const float4 *)(Raw + 4 * RW + 4 * f);
-                        const float4 x4 = *(const float4 *)(Raw + 5 * RW + 4 * f);
+                        const float4 x4 = cp.xmode ? *(const float4 *)(Raw + 5 * RW + 4 * f) : make_float4(0, 0, 0, 0);
                         const float pv[4] = {p4.x, p4.y, p4.z, p4.w}, xv[4] = {x4.x, x4.y, x4.z, x4.w};
                         float po[4], xo[4];
 #pragma unroll
                         for (int k = 0; k < 4; ++k) {
-                            po[k] = fmaf(beta, pv[k], dv[k] * rv[k]);
-                            xo[k] = fmaf(alpha, po[k], xv[k]);
+                            const float ur = dv[k] * rv[k];  // u_i = M r_i
+                            po[k] = fmaf(beta, pv[k], ur);
+                            xo[k] = cp.xmode == 2 ? fmaf(c1, pv[k], fmaf(alpha, ur, xv[k])) : fmaf(alpha, po[k], xv[k]);
                             g_ru = fmaf(rno[k], val[k], g_ru);
                             g_rr = dv[k] != 0.0f ? fmaf(rno[k], rno[k], g_rr) : g_rr;  // free DOFs only
                         }
                         *(float4 *)(cp.snew + gw) = make_float4(so[0], so[1], so[2], so[3]);
                         *(float4 *)(cp.rnew + gw) = make_float4(rno[0], rno[1], rno[2], rno[3]);
                         *(float4 *)(cp.p + gw) = make_float4(po[0], po[1], po[2], po[3]);
-                        *(float4 *)(cp.xu + gw) = make_float4(xo[0], xo[1], xo[2], xo[3]);
+                        if (cp.xmode) *(float4 *)(cp.xu + gw) = make_float4(xo[0], xo[1], xo[2], xo[3]);
                     } else if (!(in_all && own_none)) {
                         // edge group: word by word
                         const bool any_own = !own_none;
                         float pv[4] = {0.0f, 0.0f, 0.0f, 0.0f}, xv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
                         if (any_own) {
                             const float4 p4 = *(const float4 *)(Raw + 4 * RW + 4 * f);
-                            const float4 x4 = *(const float4 *)(Raw + 5 * RW + 4 * f);
                             pv[0] = p4.x, pv[1] = p4.y, pv[2] = p4.z, pv[3] = p4.w;
-                            xv[0] = x4.x, xv[1] = x4.y, xv[2] = x4.z, xv[3] = x4.w;
+                            if (cp.xmode) {
+                                const float4 x4 = *(const float4 *)(Raw + 5 * RW + 4 * f);
+                                xv[0] = x4.x, xv[1] = x4.y, xv[2] = x4.z, xv[3] = x4.w;
+                            }
                         }
 #pragma unroll
                         for (int k = 0; k < 4; ++k) {
@@ -463,11 +473,14 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                             const bool own = valid && any_own && cw >= P.olo3 && cw < P.ohi3;
                             if (!valid) val[k] = 0.0f;
                             if (own) {
-                                const float po = fmaf(beta, pv[k], dv[k] * rv[k]);
+                                const float ur = dv[k] * rv[k];
+                                const float po = fmaf(beta, pv[k], ur);
                                 cp.snew[gw + k] = so[k];
                                 cp.rnew[gw + k] = rno[k];
                                 cp.p[gw + k] = po;
-                                cp.xu[gw + k] = fmaf(alpha, po, xv[k]);
+                                if (cp.xmode)
+                                    cp.xu[gw + k] =
+                                        cp.xmode == 2 ? fmaf(c1, pv[k], fmaf(alpha, ur, xv[k])) : fmaf(alpha, po, xv[k]);
                                 g_ru = fmaf(rno[k], val[k], g_ru);
                                 g_rr = dv[k] != 0.0f ? fmaf(rno[k], rno[k], g_rr) : g_rr;
                             }
@@ -544,11 +557,12 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     // plane: the second plane's copies go out after the first plane is combined) ----------
     issue_plane(x0);
     issue_eplane(x0);
-    if (!pre(alpha, beta)) {
+    if (!pre(alpha, beta, alpha_prev)) {
         cp_async_wait_all();  // no copy may land after the CTA has left
         bulk_wait();
         return false;
     }
+    c1 = fmaf(alpha, beta, alpha_prev);  // the two-step x update's coefficient of p_{i-1}
     commit_plane(0, x0);
     __syncthreads();  // every thread's reads of the raw buffers before they are refilled
     issue_plane(x0 + 1);
@@ -728,8 +742,10 @@ __device__ __forceinline__ void cg_fold(CgState &s, const PcgScalars *sc, const 
     block_sum_df<3>(tot, sred);
     if (threadIdx.x == 0) {
         int it = s.iter, done = 0, status = s.status;
+        const df32 a_before = s.alpha;
         cg_scalar_step_df(tot[0], tot[1], tot[2], sc->rr_stop, sc->max_iter, it, done, status, s.gamma, s.alpha,
                           s.beta);
+        if (!done) s.alpha_prev = a_before;
         s.iter = it;
         s.done = done;
         s.status = status;
@@ -755,7 +771,7 @@ __global__ void __launch_bounds__(NT, 2)
     const int nblk = gridDim.x * gridDim.y;
     const int bid = blockIdx.x + gridDim.x * blockIdx.y;
     const int par = phase & 1;
-    CgPass cp{0.0f, 0.0f, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    CgPass cp{0.0f, 0.0f, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0};
     if (MODE == MODE_CG) {
         // Launch k runs iteration k while the solve lasts, so the vector parity is the launch
         // parity (and w cycles with k mod 3): the first plane's copies go out before the state
@@ -768,10 +784,11 @@ __global__ void __launch_bounds__(NT, 2)
         float *w_c = w3 == 0 ? ca.w[0] : w3 == 1 ? ca.w[1] : ca.w[2];
         float *w_n = w3 == 0 ? ca.w[1] : w3 == 1 ? ca.w[2] : ca.w[0];
         float *w_z = w3 == 0 ? ca.w[2] : w3 == 1 ? ca.w[0] : ca.w[1];
-        cp = CgPass{0.0f, 0.0f, r_c, w_c, s_n, ca.dinv, r_n, s_c, ca.p, ca.xu, w_z, ca.sc};
+        // x is updated on odd launches only, two iterations at a time
+        cp = CgPass{0.0f, 0.0f, r_c, w_c, s_n, ca.dinv, r_n, s_c, ca.p, ca.xu, w_z, ca.sc, odd ? 2 : 0};
         y = w_n;
     }
-    auto pre = [&](float &alpha, float &beta) -> bool {
+    auto pre = [&](float &alpha, float &beta, float &alpha_prev) -> bool {
         if (MODE != MODE_CG) return true;
         const PcgScalars *sc = ca.sc;
         CgState s = sc->st[par ^ 1];
@@ -786,6 +803,7 @@ __global__ void __launch_bounds__(NT, 2)
         }
         alpha = s.alpha.hi;
         beta = s.beta.hi;
+        alpha_prev = s.alpha_prev.hi;
         return !s.done;
     };
     float sums[3];

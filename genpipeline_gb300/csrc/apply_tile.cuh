@@ -29,9 +29,10 @@ enum { MODE_PLAIN = 0, MODE_PCG = 1, MODE_CG = 3, MODE_CG_FUSED = 4 };
 // State of the one-kernel PCG at the start of an iteration. Launch k writes slot k & 1 and
 // reads slot (k & 1) ^ 1; `pending` marks a state whose pass has written block partial sums
 // (slot k & 1 of the partials) that the next launch folds in before its own pass.
-// The scalars are double-float (hi, lo) pairs.
+// The scalars are double-float (hi, lo) pairs; alpha_prev is the alpha of the iteration
+// before (the odd launches' two-step update of x uses it).
 struct CgState {
-    df32 alpha, beta, gamma, rr, pap;
+    df32 alpha, beta, gamma, rr, pap, alpha_prev;
     int iter, done, status, pending;
 };
 

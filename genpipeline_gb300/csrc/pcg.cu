@@ -296,6 +296,8 @@ __global__ void cg_fold_kernel(int nblk, int last, double *partials, PcgScalars 
         sc->rr = df_value(s.rr);
         sc->pap = df_value(s.pap);
         sc->alpha[0] = df_value(s.alpha);
+        // alpha of the last launched iteration (x may still owe its step: pcg_finalize_kernel)
+        sc->alpha[1] = df_value(s.done ? s.alpha : s.alpha_prev);
         sc->beta = df_value(s.beta);
         if (sc->status == GBS_OK) sc->status = s.status;
         sc->done = sc->done || s.done;
@@ -335,12 +337,22 @@ __global__ void __launch_bounds__(256) pcg_update_kernel(int64_t nd, const float
 
 // After the loop: x = 0 when D b = 0; otherwise the dense form (lazy = 1) adds alpha_last
 // p_last (the iteration that met the stop test has not yet added its own step). The
-// single-reduction form has x complete already.
+// persistent single-reduction kernel (lazy = 0) has x complete already; the one-kernel form
+// (lazy = 2) updates x on odd launches for two iterations at once, so when the last launched
+// iteration was even (iter odd) x still owes alpha p of it (p0 holds that p, alpha[1] its
+// alpha).
 __global__ void pcg_finalize_kernel(int64_t nd, const float *p0, const float *p1, float *xu, const PcgScalars *sc,
                                     int lazy) {
     const int st = sc->status;
     const int it = sc->iter;
     const bool zero = sc->bnorm == 0.0;
+    if (lazy == 2) {
+        if (!zero && !((it & 1) && st != GBS_ENONFINITE)) return;
+        const float a = (float)sc->alpha[1];
+        for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x)
+            xu[d] = zero ? 0.0f : fmaf(a, p0[d], xu[d]);
+        return;
+    }
     if (!zero && (!lazy || it == 0 || st == GBS_EBREAKDOWN || st == GBS_ENONFINITE)) return;
     const float alpha = (float)sc->alpha[(it - 1) & 1];
     const float *p = ((it - 1) & 1) ? p1 : p0;
@@ -510,10 +522,10 @@ __global__ void __launch_bounds__(NT, 2)
     unsigned target = 0;
     while (!done) {
         const int c = it & 1, nc = c ^ 1;
-        const CgPass cp{alpha.hi, beta.hi, ca.r[c], ca.w[c], ca.s[nc], ca.dinv, ca.r[nc], ca.s[c], ca.p, ca.xu, nullptr, ca.sc};
+        const CgPass cp{alpha.hi, beta.hi, ca.r[c], ca.w[c], ca.s[nc], ca.dinv, ca.r[nc], ca.s[c], ca.p, ca.xu, nullptr, ca.sc, 1};
         float sums[3];
         modal_pass<NT, EPT, MAXV, MODE_CG_FUSED>(G, D.x, nullptr, ca.w[nc], D.mask, law, km, cp, (float *)smem4, tile, seg,
-                                                 sums, [](float &, float &) { return true; });
+                                                 sums, [](float &, float &, float &) { return true; });
         __threadfence();
         target += nblk;
         df32 tot[3];
@@ -896,7 +908,7 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
             GBS_CUDA_TRY(cudaGraphLaunch(exec, st));
             rc = cg_publish(ctx, nx, ny, nz, w, 1, st);
             if (rc) return rc;
-            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 0 : 1);
+            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 2 : 1);
             GBS_LAUNCH_CHECK("pcg_finalize_kernel");
             if (async) return GBS_OK;  // the caller counts the loop's launches from the scalars
             rc = read_scalars(w.sc, &h, st);
@@ -947,7 +959,7 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
         if (check_every <= 0 && chunk < max_chunk) chunk *= 2;
     }
     for (auto &e : ev) cudaEventDestroy(e);
-    pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 0 : 1);
+    pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 2 : 1);
     GBS_LAUNCH_CHECK("pcg_finalize_kernel");
     rc = read_scalars(w.sc, &h, st);
     if (rc) return rc;
@@ -1614,8 +1626,10 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
             const int64_t nd = n_dof_of(it.nx, it.ny, it.nz);
             SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
             PcgWs pw = pcg_ws(w.pcg, it.nx, it.ny, it.nz);
+            // one-kernel graph loop (the pending items): x may owe a half step; persistent: complete
+            const bool graph_loop = std::find(pending.begin(), pending.end(), inn[k + j]) != pending.end();
             pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, pw.p0, pw.p1, w.d32, pw.sc,
-                                                                    use_modal(ctx, it.nz) ? 0 : 1);
+                                                                    use_modal(ctx, it.nz) ? (graph_loop ? 2 : 0) : 1);
             GBS_LAUNCH_CHECK("pcg_finalize_kernel");
             GBS_CUDA_TRY(cudaMemcpyAsync((char *)hp + j * ps, pw.sc, ps, cudaMemcpyDeviceToHost, st));
         }
