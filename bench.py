@@ -41,9 +41,10 @@ WORKLOADS = {
     # 32x16x16 cantilever (8,192 elements, 28,611 DOFs), for profiling and comparison
     "c0": {"workload": "simp_32x16x16_cantilever", "grid": [32, 16, 16], "rmin": 1.5, "volfrac": 0.3,
            "load": "cantilever", "load_text": "x=0 clamped, unit -z point load at node (32, 8, 0)"},
-    # 192x96x96 (1,769,472 elements, 5,447,811 DOFs): the HBM-bound size of the apply
+    # the serving stream (run_serve): Poisson arrivals, edges 24..96, three load cases
     "serve": {"workload": "fem_serving_stream", "grid": [64, 64, 64], "rmin": 2.0, "volfrac": 0.25,
               "load": "top_patch", "load_text": "per request: cantilever tip, top patch or torsion couple"},
+    # 192x96x96 (1,769,472 elements, 5,447,811 DOFs): the PCG vectors no longer fit in L2
     "c4": {"workload": "simp_192x96x96_edge_line", "grid": [192, 96, 96], "rmin": 3.0, "volfrac": 0.2,
            "load": "edge_line",
            "load_text": "x=0 clamped, -z line load (total 1) along the bottom edge of the x=192 face"},
@@ -59,7 +60,8 @@ def _args():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="simp64")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["apply"], default="simp64",
+                    help="simp64 (the bench line), c0, c4, serve, or apply (the bare stiffness apply)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-steps", type=int, default=1)
     ap.add_argument("--serve-requests", type=int, default=2000)
@@ -360,6 +362,78 @@ def measure_rows(xphys64=None):
     return rows
 
 
+def run_apply(a):
+    """The bare stiffness apply y = D K(x) D p (`apply_modal_kernel<PLAIN>`, no masks) at 64^3
+    and 192x96x96 on seeded densities U(0.1, 1) and a seeded N(0, 1) vector. Warm: 20
+    back-to-back launches, median of 5 groups. Cold: single launches after a 256 MB L2 flush,
+    median of `--steps` (at least 5). Algorithmic bytes are 4*(2 n_dof + n_elem): p in, y out,
+    the densities in."""
+    import torch
+
+    from genpipeline_gb300 import _lib as L
+    from genpipeline_gb300.engine import Engine, n_dof, n_elem
+
+    lib = L.load()
+    eng = Engine()
+    law = L.make_law("modified", 3.0)
+    flush = torch.empty(256 * 2**20, dtype=torch.uint8, device="cuda")
+    peak, peak_src = _measured_peak()
+    n_cold = max(5, a.steps)
+
+    def timed(fn):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3
+
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    l0 = lib.gbsimp_launch_count()
+    grids = {}
+    for grid in [(64, 64, 64), (192, 96, 96)]:
+        ne, nd = n_elem(grid), n_dof(grid)
+        gen = torch.Generator(device="cuda").manual_seed(0)
+        x = torch.rand(ne, device="cuda", generator=gen) * 0.9 + 0.1
+        p = torch.randn(nd, device="cuda", generator=gen)
+        y = torch.empty_like(p)
+        for _ in range(max(3, a.warmup)):
+            eng.apply(grid, law, x, p, None, y)
+        torch.cuda.synchronize()
+
+        def burst():
+            for _ in range(20):
+                eng.apply(grid, law, x, p, None, y)
+
+        warm = statistics.median(timed(burst) / 20 for _ in range(5))
+        cold = []
+        for _ in range(n_cold):
+            flush.zero_()
+            cold.append(timed(lambda: eng.apply(grid, law, x, p, None, y)))
+        cold = statistics.median(cold)
+        alg = 4 * (2 * nd + ne)
+        grids["x".join(map(str, grid))] = {
+            "path": eng.apply_path(grid[2]), "alg_bytes": alg, "warm_us": warm * 1e6, "cold_us": cold * 1e6,
+            "cold_GBs": alg / cold / 1e9, "cold_frac": alg / cold / 1e9 / peak,
+            "dense_equiv_tflops": 1152 * ne / cold / 1e12}
+    launches = lib.gbsimp_launch_count() - l0
+    clk = clocks.stop()
+    c4 = grids["192x96x96"]
+    line = {"metric": "stiffness apply y = K(x) p, algorithmic GB/s (192x96x96, L2 flushed)",
+            "value": c4["cold_GBs"], "unit": "GB/s", "n_gpus": 1, "steps": n_cold, "warmup": max(3, a.warmup),
+            "ms_per_step": c4["cold_us"] * 1e-3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "ours",
+            "config": {"workload": "stiffness_apply", "grids": list(grids), "densities": "U(0.1, 1), seed 0",
+                       "law": COMMON["law"], "l2": "flushed (256 MB write) before each cold launch"},
+            "roofline": {"bound": "hbm", "kernel": "apply_modal_kernel<PLAIN>", "achieved": c4["cold_GBs"],
+                         "peak": peak, "peak_source": peak_src, "unit": "GB/s", "frac": c4["cold_frac"],
+                         "traffic": None},
+            "grids": grids, "gpu_launches": int(launches), "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def run_serve(a):
     """Serving stream: Poisson arrivals at 200/s, edge U{24,32,48,64,96}, three load cases,
     ~10% repeated designs; continuous batching with admission by free HBM."""
@@ -586,10 +660,14 @@ def run_reference(a):
 
 def main():
     a = _args()
+    if a.workload == "apply" and a.impl == "reference":
+        sys.exit("bench.py: --workload apply has no reference arm (the reference times whole SIMP iterations)")
     if a.impl == "reference":
         run_reference(a)
     elif a.workload == "serve":
         run_serve(a)
+    elif a.workload == "apply":
+        run_apply(a)
     else:
         run_ours(a)
 
