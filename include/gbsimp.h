@@ -349,7 +349,8 @@ int gbsimp_marching_cubes(gbsimp_ctx *ctx, int nx, int ny, int nz, const float *
                           int64_t *n_tris, void *ws, size_t ws_bytes, void *stream);
 /* The case table the kernel uses (host memory, no GPU needed): per case the triangle count
  * (ntri[256]), loop count (nloop[256]), loop lengths (len[256][4]) and the loops' cut-edge
- * indices (edge[256][12]). Any pointer may be NULL. Returns the largest triangle count. */
+ * indices (edge[256][12]). Any pointer may be NULL. Returns an upper bound on any case's
+ * triangle count: 12, the number of cell edges (a loop of n cut edges gives at most n). */
 int gbsimp_marching_cubes_table(unsigned char *ntri, unsigned char *nloop, unsigned char *len,
                                 signed char *edge);
 

@@ -61,6 +61,27 @@ def test_workspace_queries_are_host_only():
     assert lib.gbsimp_pcg_csr_ws_bytes(1000) >= 16000
 
 
+def test_every_status_entry_point_rejects_null_arguments():
+    """Every status-returning call, given a NULL context, zero sizes and NULL pointers, returns
+    GBS_EINVAL with a message before touching the device (no GPU here)."""
+    lib = L.load()
+    no_status = {"gbsimp_abi_version", "gbsimp_launch_count", "gbsimp_last_error", "gbsimp_create",
+                 "gbsimp_destroy", "gbsimp_queue_destroy", "gbsimp_queue_size", "gbsimp_apply_path",
+                 "gbsimp_marching_cubes_table"}
+    checked = 0
+    for name, (res, args) in sorted(L.SIGNATURES.items()):
+        if name in no_status or res is not L._I:
+            continue
+        vals = [0 if a in (L._I, L._I64, L._SZ, C.c_int32) else 0.0 if a is L._D else None for a in args]
+        assert getattr(lib, name)(*vals) == L.GBS_EINVAL, name
+        assert lib.gbsimp_last_error(), name
+        checked += 1
+    assert checked >= 28
+    assert lib.gbsimp_apply_path(None, 64) == -1
+    ntri = (C.c_ubyte * 256)()
+    assert lib.gbsimp_marching_cubes_table(ntri, None, None, None) == 12 >= max(ntri) > 0
+
+
 def test_queue_and_simp_run_argument_checks_without_gpu():
     """Host-only paths of the queue and the SIMP loop: size queries and argument errors."""
     lib = L.load()
