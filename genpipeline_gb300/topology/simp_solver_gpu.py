@@ -18,6 +18,7 @@ is (:793).
 """
 from __future__ import annotations
 
+import pickle
 from dataclasses import dataclass
 
 import numpy as np
@@ -41,6 +42,43 @@ class MatrixFreeK:
     def shape(self):
         nd = n_dof(self.grid)
         return (nd, nd)
+
+
+class _BcCache:
+    """The boundary conditions of one (grid, boundary_conditions, force) on the device, and the
+    node mask of the last fixed-DOF set seen. The reference rebuilds both on the host twice per
+    SIMP iteration (its sensitivity solve and its compliance solve), which at 64^3 costs about
+    8 ms per build against about 6 ms of device work per iteration."""
+
+    def __init__(self, grid, device):
+        self.grid = tuple(grid)
+        self.device = device
+        self._key = None
+        self._f = self._fixed = None
+        self._mask_fixed = self._mask = None
+
+    def bcs(self, bcs: dict, force_mag: float):
+        """Copies of the cached (f FP64, fixed_dofs int64), rebuilt when `bcs` or the force
+        changes (the caller gets tensors of its own, as from a fresh build)."""
+        try:
+            key = (float(force_mag), pickle.dumps(sorted(bcs.items())))
+        except Exception:  # values that cannot be compared: build every call
+            key = None
+        if key is None or key != self._key:
+            f, fixed = B.reference_gpu(*self.grid, bcs, force_mag)
+            self._f = torch.as_tensor(f, dtype=torch.float64, device=self.device)
+            self._fixed = torch.as_tensor(fixed, dtype=torch.int64, device=self.device)
+            self._key = key
+        return self._f.clone(), self._fixed.clone()
+
+    def mask(self, fixed_dofs) -> torch.Tensor:
+        """Per-node Dirichlet bits of `fixed_dofs`, rebuilt only when the set differs from the
+        last one (compared on the device)."""
+        fd = torch.as_tensor(fixed_dofs, device=self.device).reshape(-1).to(torch.int64)
+        if self._mask is None or not torch.equal(self._mask_fixed, fd):
+            self._mask = torch.as_tensor(B.node_mask(*self.grid, fd.detach().cpu().numpy()), device=self.device)
+            self._mask_fixed = fd.clone()
+        return self._mask
 
 
 class SIMPSolverGPU:
@@ -74,6 +112,7 @@ class SIMPSolverGPU:
         self.bcs = {"fixed_face": "x_min", "load_face": "x_max", "load_dof": 2}
         if boundary_conditions:
             self.bcs.update(boundary_conditions)
+        self._bc_cache = _BcCache(self.grid, self.device)
         self._u_prev = None
         self._law = L.make_law("ref", penal)
         self._oc_key = f"ocgpu:{id(self)}"
@@ -82,18 +121,16 @@ class SIMPSolverGPU:
 
     # ---- internals with the reference's names -------------------------------------------
     def _get_bcs(self, force_mag: float):
-        """(f, fixed_dofs) as device tensors, simp_solver_gpu.py:138-248."""
-        f, fixed = B.reference_gpu(self.nx, self.ny, self.nz, self.bcs, force_mag)
-        return (torch.as_tensor(f, dtype=torch.float64, device=self.device),
-                torch.as_tensor(fixed, dtype=torch.int64, device=self.device))
+        """(f, fixed_dofs) as device tensors, simp_solver_gpu.py:138-248 (built once per
+        boundary conditions and force, then copied on the device)."""
+        return self._bc_cache.bcs(self.bcs, force_mag)
 
     def _assemble_K(self, xPhys: torch.Tensor) -> MatrixFreeK:
         x = torch.as_tensor(xPhys, device=self.device).reshape(-1).to(torch.float32).contiguous()
         return MatrixFreeK(x, L.make_law("ref", self.penal), self.grid)
 
     def _mask(self, fixed_dofs: torch.Tensor) -> torch.Tensor:
-        return torch.as_tensor(B.node_mask(self.nx, self.ny, self.nz, fixed_dofs.detach().cpu().numpy()),
-                               device=self.device)
+        return self._bc_cache.mask(fixed_dofs)
 
     def _solve(self, K: MatrixFreeK, f: torch.Tensor, fixed_dofs: torch.Tensor, tol: float = 1e-6,
                max_iter: int = 2000, x0: torch.Tensor | None = None) -> torch.Tensor:

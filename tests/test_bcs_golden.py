@@ -67,3 +67,28 @@ def test_cantilever_point_location():
     (d,) = np.flatnonzero(f)
     assert d == 3 * bcs.node_id(32, 8, 0, 16, 16) + 2 and f[d] == -1.0
     assert len(fixed) == 3 * 17 * 17
+
+
+def test_solver_bc_cache_equals_a_fresh_build():
+    """SIMPSolverGPU's device cache of its boundary conditions (exercised on CPU tensors):
+    every call equals a fresh host build, hands out tensors of its own, and follows changes of
+    the force and of the boundary-condition dictionary; the node mask follows the fixed set."""
+    import torch
+
+    from genpipeline_gb300.topology.simp_solver_gpu import _BcCache
+
+    grid = (7, 3, 8)
+    cache = _BcCache(grid, torch.device("cpu"))
+    spec = {"fixed_face": "x_min", "load_face": "x_max", "load_dof": 2}
+    for force, spec_now in ((2.5, spec), (2.5, spec), (1.0, spec), (1.0, dict(spec, load_dof=1)),
+                            (1.0, dict(spec, fixed_face=["x_min", "z_min"])), (1.0, spec)):
+        f, fixed = cache.bcs(spec_now, force)
+        f_ref, fixed_ref = bcs.reference_gpu(*grid, spec_now, force)
+        np.testing.assert_array_equal(f.numpy(), f_ref)
+        np.testing.assert_array_equal(fixed.numpy(), fixed_ref)
+        assert f.dtype == torch.float64 and fixed.dtype == torch.int64
+        f.mul_(7.0)  # the caller's copy: the next call is unaffected
+        np.testing.assert_array_equal(cache.mask(fixed).numpy(), bcs.node_mask(*grid, fixed_ref))
+    np.testing.assert_array_equal(cache.bcs(spec, 1.0)[0].numpy(), bcs.reference_gpu(*grid, spec, 1.0)[0])
+    other = np.array([0, 1, 2, 30], dtype=np.int64)
+    np.testing.assert_array_equal(cache.mask(torch.as_tensor(other)).numpy(), bcs.node_mask(*grid, other))
