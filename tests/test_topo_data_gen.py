@@ -1,6 +1,9 @@
-"""The data generator's draws (CPU): geometry table, weights and the per-sample draw order of
-topology/topo_data_gen.py:41-126,168-245 with numpy's global generator."""
+"""The data generator on CPU: geometry table, weights and the per-sample draw order of
+topology/topo_data_gen.py:41-126,168-245 with numpy's global generator; the batching, the
+sample records (:246-289) and the skip-on-failure rule (:301-307) with the device steps
+replaced by host stand-ins."""
 import numpy as np
+import pytest
 
 from genpipeline_gb300.topology.topo_data_gen import TopoDataGenerator
 
@@ -44,6 +47,61 @@ def test_draw_order_matches_reference(tmp_path):
         for c, (geom, dims, vf, force) in zip(ours, ref):
             assert c.tag == geom and c.grid == dims and c.volfrac == vf and c.force_mag == force
             assert c.bcs == g.GEOM_BCS[geom] and c.penal == 3.5 and c.rmin == 1.5
+
+
+def _fake_pipeline(monkeypatch, g, fail_tags=()):
+    """Replaces the device steps (batched SIMP, STL export) by host stand-ins; records the
+    batches that reach the solver."""
+    import genpipeline_gb300.topology.topo_data_gen as T
+
+    batches = []
+
+    def solve(cases):
+        batches.append([c.grid for c in cases])
+        for k, c in enumerate(cases):
+            c.density = np.full(c.grid, 0.25 + 0.01 * k)
+            c.last_compliance = 40.0 + k
+            c.failed = c.tag in fail_tags
+        return cases
+
+    def stl(density, path, threshold=0.5, voxel_size_mm=None):
+        open(path, "wb").close()
+        return path
+
+    monkeypatch.setattr(g, "_solve", solve)
+    monkeypatch.setattr(T, "density_to_stl", stl)
+    return batches
+
+
+@pytest.mark.parametrize("method", ["generate", "generate_scaled"])
+def test_generate_batches_records_and_failures(tmp_path, monkeypatch, method):
+    """generate / generate_scaled split the samples into batches, consume the draws in the
+    reference's order, write the reference's JSON record per sample and skip a failed
+    sample (logged, not raised), returning the number written."""
+    import json
+
+    g = TopoDataGenerator(output_dir=str(tmp_path), batch_size=3)
+    np.random.seed(77)
+    expect = [g._draw() for _ in range(7)]
+    fail = {expect[4].tag}
+    batches = _fake_pipeline(monkeypatch, g, fail_tags=fail)
+    np.random.seed(77)
+    n = g.generate(7) if method == "generate" else g.generate_scaled(7, batch_size=3)
+    assert batches == [[c.grid for c in expect[:3]], [c.grid for c in expect[3:6]], [expect[6].grid]]
+    kept = [(i, c) for i, c in enumerate(expect) if c.tag not in fail]
+    assert n == len(kept) == len(g.written)
+    for rec, (i, c) in zip(g.written, kept):
+        data = json.loads(open(rec["json"]).read())
+        nx, ny, nz = c.grid
+        assert data["compliance"] == 40.0 + i % 3  # the stand-in solver's value for this sample
+        assert data["stress_max"] == pytest.approx(0.1 * data["compliance"], rel=1e-15)
+        assert data["parameters"] == {"geometry": c.tag, "volfrac": c.volfrac, "force_n": c.force_mag,
+                                      "nx": nx, "ny": ny, "nz": nz, "penal": 3.5}
+        box = 100.0 * 20.0 * (100.0 if c.tag in ("lbracket", "bridge", "arch") else 20.0)
+        assert data["mass"] == pytest.approx((0.25 + 0.01 * (i % 3)) * box * 1.05e-6, rel=1e-12)
+        stem = f"{c.tag[:4]}_v{int(c.volfrac * 100)}_f{int(c.force_mag)}_{nx}x{ny}x{nz}_"
+        assert rec["stl"].rsplit("/", 1)[1].startswith(stem) and rec["stl"].endswith("_mesh.stl")
+        assert rec["json"].endswith("_fem_results.json")
 
 
 def test_generator_bcs_cover_every_geometry(tmp_path):
