@@ -6,7 +6,8 @@ budget -- by taking its scratch from a static array inside the library. It must 
 results of gbsimp_oc (which uses a caller-provided workspace) on every call, including
 consecutive calls that leave the shared array holding the previous call's contents.
 
-This file sorts last so that a run stopping at its first failure has run every other test.
+This file sorts after the other kernel tests (only the full-size checks follow it), so that a
+run stopping at its first failure has run them.
 """
 import ctypes as C
 
