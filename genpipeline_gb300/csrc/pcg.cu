@@ -5,9 +5,10 @@
 // ||r|| < rtol ||D b||):
 // - modal element (isotropic cube Ke): one launch per iteration, the single-reduction form
 //   (apply_modal.cuh, MODE_CG): the staging of the apply operand u_{i+1} = M r_{i+1} also
-//   forms s_i and r_{i+1}, the owned nodes update p and x, and the block sums of r.u, w.u and
-//   r.r give beta_{i+1} and alpha_{i+1} in the last block. Setup: r_0, u_0, w_0 = A u_0,
-//   alpha_0 = (r_0.u_0) / (w_0.u_0).
+//   forms s_i and r_{i+1}, the owned nodes update p (and x on odd launches, two iterations
+//   at once), and each block writes its sums of r.u, w.u and r.r; the next launch folds them
+//   at its start (every block, in block order) into beta_{i+1} and alpha_{i+1}. Setup: r_0,
+//   u_0, w_0 = A u_0, alpha_0 = (r_0.u_0) / (w_0.u_0).
 // - dense element (any other Ke): two launches per iteration k (setup r_0, p_{-1} = 0):
 //   K1  apply_tile_kernel<MODE_PCG>: p_k = z_k + beta_k p_{k-1} on the halo while staging,
 //       x += alpha_{k-1} p_{k-1} on owned nodes, Ap_k = D K D p_k, p_k.Ap_k -> alpha_k.
@@ -396,7 +397,6 @@ static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const La
     return GBS_OK;
 }
 
-// FP32 PCG. u: x0 in, solution out. Returns GBS_OK and fills *out (status inside).
 // ---- persistent fused PCG: the whole solve in one cooperative launch ---------------------
 // Every CTA keeps its (flat tile, x segment) of the modal apply for all iterations. One
 // iteration = the single-reduction pass (apply_modal.cuh, MODE_CG_FUSED) -> one grid barrier
@@ -871,6 +871,7 @@ struct ApplyProfile {
     int launches = 0;
 };
 
+// FP32 PCG. u: x0 in, solution out. Returns GBS_OK and fills *out (status inside).
 // With out == nullptr (and no profiling) the solve is only enqueued: the device-driven paths
 // need no host decision, and the caller reads the scalars later (w.sc of the workspace),
 // together with its own.
