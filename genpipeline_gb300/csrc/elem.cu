@@ -1,6 +1,7 @@
 // elem.cu -- element-wise kernels: sensitivity/compliance, density filter, OC bisection,
-// FP64 dot. All reductions: per-block FP64 partials, summed in block order by the last
-// block to finish (deterministic for a given launch shape).
+// FP64 dot. All reductions: per-block partials (FP64; double-float in the OC multisection),
+// summed in a fixed order by the last block to finish (deterministic for a given launch
+// shape).
 #include <math.h>
 #include <string.h>
 
@@ -49,8 +50,9 @@ inline unsigned reduce_blocks(const gbsimp_ctx *ctx, int64_t n, int threads) {
 }
 
 // ---- sensitivity ------------------------------------------------------------------------
-// Thread per element: u_e gathered in FP64 (minus node 0's displacement when Ke annihilates
-// translations), ce = u_e^T Ke u_e, dc = -dE/dx ce, energy partial E ce.
+// Thread per element: u_e gathered in FP64; ce = u_e^T Ke u_e through the modal form
+// (q = T^T u_e, the 45 nonzeros of Km) when Ke has it, else the dense product (minus node 0's
+// displacement when Ke annihilates translations); dc = -dE/dx ce, energy partial E ce.
 __global__ void __launch_bounds__(128) sens_kernel(int nx, int ny, int nz, Law<double> law, const KeD ke, int sub,
                                                    int modal, const ModalKD kmd,
                                                    const float *__restrict__ x, const double *__restrict__ u,
