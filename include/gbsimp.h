@@ -188,7 +188,7 @@ int gbsimp_oc_result(gbsimp_ctx *ctx, const void *ws, double *lambda_out, int *s
 /* FP32 Jacobi-PCG on the free DOFs (simp_solver_gpu.py:328-379, _solve :571-705):
  * u holds x0 on entry (fixed DOFs are zeroed), the solution on exit. The stop test is
  * ||r|| < rtol ||D b||, checked on the device every iteration. The iteration loop runs on
- * the device: a CUDA graph (cached per buffer set) whose WHILE node repeats 8 iterations
+ * the device: a CUDA graph (cached per buffer set) whose WHILE node repeats 12 iterations
  * while the device-side stop flag is clear, with a hard cap derived from max_iter
  * (GBS_ETIMEOUT). With opts->profile the host launches the iterations instead, checking
  * every opts->check_every iterations, and times each apply launch. Synchronises the stream. */
@@ -197,11 +197,13 @@ int gbsimp_pcg_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *la
                    const float *x, const float *b, const uint8_t *node_mask, float *u,
                    const gbsimp_solve_opts *opts, gbsimp_solve_stats *stats, void *ws,
                    size_t ws_bytes, void *stream);
-/* Measures the fused PCG apply kernel (the apply that also forms p = z + beta p, updates
- * the iterate and reduces p.Ap -- the kernel that dominates gbsimp_pcg_f32 and
- * gbsimp_solve) on the densities x: reps back-to-back launches replayed from one CUDA graph
- * and timed with CUDA events on the stream. Writes the mean device time per launch.
- * Synchronises the stream. */
+/* Measures the kernel that dominates gbsimp_pcg_f32 and gbsimp_solve on the densities x:
+ * one whole PCG iteration in one launch (modal element: the single-reduction pass that
+ * stages s, r and u = M r, applies K to u, updates p and the iterate and sums r.u, w.u and
+ * r.r; dense element: the apply fused with p = z + beta p, the iterate update and p.Ap),
+ * with frozen scalars. reps back-to-back launches replayed from one CUDA graph, timed with
+ * CUDA events on the stream; writes the mean device time per launch. Synchronises the
+ * stream. */
 size_t gbsimp_time_pcg_apply_ws_bytes(int nx, int ny, int nz);
 int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
                           const float *x, const uint8_t *node_mask, int reps, void *ws,
