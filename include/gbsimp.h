@@ -234,10 +234,12 @@ typedef struct gbsimp_batch_item {
 } gbsimp_batch_item;
 
 /* One round of the FP64 defect correction for every active item: FP64 residuals (one sync
- * for all), then ONE cooperative launch of a persistent kernel that iterates the FP32 PCG of
- * every item still above rtol (each item on its own share of the SMs, with its own grid
- * barrier and scalars, converging independently; up to 24 items per launch), then the FP64
- * corrections. Items may be added (state 0) or dropped between rounds: the serving loop's
+ * for all), then the FP32 PCG of every item still above rtol, then the FP64 corrections.
+ * With opts->fused the PCGs run as cooperative launches of a persistent kernel, up to 24
+ * items per launch, each item on its own share of the SMs with its own grid barrier and
+ * scalars, converging independently. A group whose items cannot all be resident at once,
+ * or any item when opts->fused is 0, runs its own device-driven graph loop instead, enqueued
+ * on the same stream. Items may be added (state 0) or dropped between rounds: the serving loop's
  * continuous batching. Replaces one gbsimp_solve per design (the reference's one solve per
  * GPUVoxelFEM.solve, gpu_fem_solver.py:76-133, fed by evaluate_batch's thread pool,
  * voxel_fem.py:559-611). Synchronises the stream. */
