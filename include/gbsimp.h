@@ -67,9 +67,10 @@ typedef struct gbsimp_solve_opts {
     double rtol;          /* stop when ||D(f - K u)|| <= rtol * ||D f|| (FP64 residual) */
     double inner_rtol;    /* FP32 PCG reduction per outer correction (gbsimp_solve, batch); <= 0: 1e-4 */
     int32_t max_iter;     /* cap on the total FP32 PCG iterations */
-    int32_t max_outer;    /* cap on FP64 defect corrections (gbsimp_solve only) */
-    int32_t check_every;  /* iterations between host-side convergence checks (0 = auto) */
-    int32_t fused;        /* 1 = persistent fused PCG kernel, 0 = one launch per step */
+    int32_t max_outer;    /* cap on FP64 defect corrections (gbsimp_solve, batched rounds) */
+    int32_t check_every;  /* iterations between the host's checks where the host drives the
+                             loop (profile, the CSR PCG); 0 = auto */
+    int32_t fused;        /* 1 = persistent fused PCG kernel, 0 = graph loop, one launch per iteration */
     int32_t profile;      /* 1 = time every PCG apply launch with CUDA events (stats) */
     int32_t reserved;
 } gbsimp_solve_opts;
