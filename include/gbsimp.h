@@ -256,7 +256,10 @@ int gbsimp_batch_solve(gbsimp_ctx *ctx, gbsimp_batch_item *items, int n, const g
  * design (voxel_fem.py:559-611 over gpu_fem_solver.py:76-133) for a serving loop: requests
  * join between rounds as they arrive and leave when they are done. The queue keeps pointers to
  * the submitted items; their buffers and workspaces stay the caller's until poll returns
- * them. All items of a queue share the law and the solve options given at creation. */
+ * them. All items of a queue share the law and the solve options given at creation.
+ * submit, poll and size may be called from different threads: each takes the queue's lock,
+ * and poll holds it for its whole round, so a submit during a round waits for that round
+ * and joins the next. */
 typedef struct gbsimp_queue gbsimp_queue;
 int gbsimp_queue_create(gbsimp_ctx *ctx, const gbsimp_law *law, const gbsimp_solve_opts *opts,
                         gbsimp_queue **out);
