@@ -845,11 +845,17 @@ inline ModalGeom modal_geom(int nx, int ny, int nz, int num_sms, int blocks_per_
     return g;
 }
 
-inline dim3 modal_grid(const ModalGeom &g) {
-    const int NE = kModalNT * kModalEPT, H = g.nz + 2, F = NE - H;
-    const int S = (g.ny + 1) * (g.nz + 1);
-    return dim3((unsigned)((S + F - 1) / F), (unsigned)g.nseg, 1);
+// Flat tiles of one (y, z) node plane: the CTAs of one x segment (modal_fits(nz) holds).
+inline int modal_tiles(int ny, int nz) {
+    const int F = kModalNT * kModalEPT - (nz + 2);
+    return ((ny + 1) * (nz + 1) + F - 1) / F;
 }
+
+// Upper bound on one wave of resident modal CTAs (SMs x CTAs per SM) that workspaces are
+// sized for; a launch of max(tiles, wave) CTAs beyond what a workspace holds is refused.
+constexpr int kModalMaxWave = 2048;
+
+inline dim3 modal_grid(const ModalGeom &g) { return dim3((unsigned)modal_tiles(g.ny, g.nz), (unsigned)g.nseg, 1); }
 
 // 16-byte groups of a staged plane per thread: 2 when 4 * ceil((3R + 3) / 4) <= 8 NT words
 // (nz <= 166), else 3 (modal_fits bounds nz).

@@ -53,10 +53,28 @@ struct PcgWs {
 
 static inline bool use_modal(const gbsimp_ctx *ctx, int nz) { return ctx->modal_ok && modal_fits(nz); }
 
+// Partial sums (8 bytes each) of the workspace: one per CTA of the dense form; two slots of
+// three per CTA of the one-kernel PCG, whose launch has tiles x segments <= max(tiles,
+// one wave) CTAs (checked in pcg_setup); three per block of the vector reductions.
 static size_t pcg_partials(int nx, int ny, int nz) {
     const dim3 g = tile_grid<TileF>(nx, ny, nz);
     size_t n = (size_t)g.x * g.y * g.z;
+    if (modal_fits(nz)) {
+        const int t = modal_tiles(ny, nz);
+        const size_t m = 6 * (size_t)(t > kModalMaxWave ? t : kModalMaxWave);
+        if (m > n) n = m;
+    }
     return n > 3 * 4096 ? n : 3 * 4096;
+}
+
+// The one-kernel PCG's launch on this grid writes 6 partial sums per CTA: refuse a workspace
+// that cannot hold them (a wave larger than kModalMaxWave CTAs).
+static int check_modal_partials(const gbsimp_ctx *ctx, int nx, int ny, int nz, const PcgWs &w) {
+    const int nblk = modal_blocks<MODE_CG>(ctx, nx, ny, nz);
+    if (nblk < 0) return -nblk;
+    if (6 * (size_t)nblk > w.partial_count)
+        return set_error(GBS_EINVAL, "PCG: the launch needs more partial sums than the workspace holds");
+    return GBS_OK;
 }
 
 static size_t pcg_ws_bytes_impl(int nx, int ny, int nz) {
@@ -826,6 +844,10 @@ static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp
                      cudaStream_t st, unsigned flags = 0) {
     const int64_t nd = n_dof_of(nx, ny, nz);
     const Law<float> law = make_law<float>(*glaw);
+    if (use_modal(ctx, nz)) {
+        const int rc = check_modal_partials(ctx, nx, ny, nz, w);
+        if (rc) return rc;
+    }
     GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
     if (!(flags & SETUP_KEEP_DINV)) {
         dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, law, ctx->kef, x, mask, w.dinv);
@@ -1337,6 +1359,10 @@ extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, co
     // r = 1, everything else 0 (alpha = beta = 0), iteration 0. Single-reduction kernel: the
     // scalars are frozen, so no launch advances the iteration. Dense form: K2 never runs.
     const bool modal = use_modal(ctx, nz);
+    if (modal) {
+        const int rc = check_modal_partials(ctx, nx, ny, nz, w);
+        if (rc) return rc;
+    }
     GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
     dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, law, ctx->kef, x, node_mask, w.dinv);
     fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 1.0f, w.r);

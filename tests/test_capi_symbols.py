@@ -61,6 +61,32 @@ def test_workspace_queries_are_host_only():
     assert lib.gbsimp_pcg_csr_ws_bytes(1000) >= 16000
 
 
+def test_pcg_workspace_holds_the_one_kernel_partials():
+    """The one-kernel PCG writes two slots of three partial sums (8 bytes each) per CTA; its
+    launch is tiles x segments CTAs, tiles = ceil((ny+1)(nz+1) / (512 - (nz+2))) per plane and
+    segments filling one wave (at least one). The workspace's partials region must hold them
+    for waves up to 2048 CTAs, including planes of thousands of tiles (large ny with nz near
+    the modal limit of 446)."""
+    lib = L.load()
+
+    def al(b):
+        return (b + 255) // 256 * 256
+
+    sc = lib.gbsimp_pcg_ws_bytes(1, 1, 1) - 256 - 9 * al(4 * 24) - al(8 * 12288)  # the scalars block
+    assert sc > 0 and sc % 256 == 0
+    rng = np.random.default_rng(0)
+    shapes = [(64, 64, 64), (192, 96, 96), (1, 300, 446), (2, 2000, 446), (1, 600, 400), (3, 1, 446), (1, 1, 1)]
+    shapes += [(int(rng.integers(1, 64)), int(rng.integers(1, 2500)), int(rng.integers(1, 447))) for _ in range(300)]
+    for nx, ny, nz in shapes:
+        nd = 3 * (nx + 1) * (ny + 1) * (nz + 1)
+        part = lib.gbsimp_pcg_ws_bytes(nx, ny, nz) - 256 - sc - 9 * al(4 * nd)
+        f = 512 - (nz + 2)
+        tiles = -(-(ny + 1) * (nz + 1) // f)
+        for wave in (1, 152, 304, 608, 2048):
+            nblk = tiles * max(1, min(wave // tiles, nx))
+            assert part >= 48 * nblk, (nx, ny, nz, wave)
+
+
 def test_every_status_entry_point_rejects_null_arguments():
     """Every status-returning call, given a NULL context, zero sizes and NULL pointers, returns
     GBS_EINVAL with a message before touching the device (no GPU here)."""
