@@ -858,7 +858,7 @@ constexpr int kModalMaxWave = 2048;
 inline dim3 modal_grid(const ModalGeom &g) { return dim3((unsigned)modal_tiles(g.ny, g.nz), (unsigned)g.nseg, 1); }
 
 // 16-byte groups of a staged plane per thread: 2 when 4 * ceil((3R + 3) / 4) <= 8 NT words
-// (nz <= 166), else 3 (modal_fits bounds nz).
+// (nz <= 167), else 3 (modal_fits bounds nz).
 inline bool modal_short(int nz) { return (3 * (kModalNT * kModalEPT + nz + 2) + 6) / 4 <= 2 * kModalNT; }
 
 // Resident CTAs per SM of a kernel that uses `smem` bytes of dynamic shared memory: the
