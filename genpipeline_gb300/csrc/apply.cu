@@ -97,7 +97,7 @@ using namespace gbs;
 
 extern "C" int gbsimp_apply_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
                                 const float *p, float *y, const uint8_t *node_mask, void *stream) {
-    if (!ctx || !law || !x || !p || !y || nx <= 0 || ny <= 0 || nz <= 0)
+    if (!ctx || !law || !x || !p || !y || !grid_ok(nx, ny, nz))
         return set_error(GBS_EINVAL, "gbsimp_apply_f32: bad arguments");
     return apply_f32(ctx, nx, ny, nz, law, x, p, y, node_mask, (cudaStream_t)stream);
 }
@@ -109,7 +109,7 @@ extern "C" int gbsimp_apply_path(const gbsimp_ctx *ctx, int nz) {
 
 extern "C" int gbsimp_apply_f64(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
                                 const double *p, double *y, const uint8_t *node_mask, void *stream) {
-    if (!ctx || !law || !x || !p || !y || nx <= 0 || ny <= 0 || nz <= 0)
+    if (!ctx || !law || !x || !p || !y || !grid_ok(nx, ny, nz))
         return set_error(GBS_EINVAL, "gbsimp_apply_f64: bad arguments");
     return apply_f64(ctx, nx, ny, nz, law, x, p, y, node_mask, (cudaStream_t)stream);
 }

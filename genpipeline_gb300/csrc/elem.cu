@@ -521,7 +521,7 @@ extern "C" size_t gbsimp_sensitivity_ws_bytes(int nx, int ny, int nz) {
 extern "C" int gbsimp_sensitivity(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
                                   const double *u, float *dc, float *ce, double *energy_out, void *ws,
                                   size_t ws_bytes, void *stream) {
-    if (!ctx || !law || !x || !u || nx <= 0 || ny <= 0 || nz <= 0)
+    if (!ctx || !law || !x || !u || !grid_ok(nx, ny, nz))
         return set_error(GBS_EINVAL, "gbsimp_sensitivity: bad arguments");
     if (energy_out && (!ws || ws_bytes < gbsimp_sensitivity_ws_bytes(nx, ny, nz)))
         return set_error(GBS_EINVAL, "gbsimp_sensitivity: workspace too small");
@@ -538,13 +538,13 @@ extern "C" int gbsimp_sensitivity(gbsimp_ctx *ctx, int nx, int ny, int nz, const
 }
 
 extern "C" int gbsimp_filter_hs(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, float *hs, void *stream) {
-    if (!ctx || !hs || nx <= 0 || ny <= 0 || nz <= 0) return set_error(GBS_EINVAL, "gbsimp_filter_hs: bad arguments");
+    if (!ctx || !hs || !grid_ok(nx, ny, nz)) return set_error(GBS_EINVAL, "gbsimp_filter_hs: bad arguments");
     return filter_launch(ctx, nx, ny, nz, rmin, 2, nullptr, nullptr, nullptr, hs, (cudaStream_t)stream);
 }
 
 extern "C" int gbsimp_filter(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const float *hs, const float *in,
                              float *out, int transpose, void *stream) {
-    if (!ctx || !in || !out || nx <= 0 || ny <= 0 || nz <= 0)
+    if (!ctx || !in || !out || !grid_ok(nx, ny, nz))
         return set_error(GBS_EINVAL, "gbsimp_filter: bad arguments");
     if (transpose && !hs) return set_error(GBS_EINVAL, "gbsimp_filter: the transpose needs hs");
     return filter_launch(ctx, nx, ny, nz, rmin, transpose ? 1 : 0, hs, in, nullptr, out, (cudaStream_t)stream);
@@ -605,7 +605,7 @@ int oc_run_impl(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, cons
 
 int oc_check_args(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_oc_params *prm, const float *x,
                   const float *dc, const float *xnew, const float *xphys) {
-    if (!ctx || !prm || !x || !dc || !xnew || !xphys || nx <= 0 || ny <= 0 || nz <= 0)
+    if (!ctx || !prm || !x || !dc || !xnew || !xphys || !grid_ok(nx, ny, nz))
         return set_error(GBS_EINVAL, "gbsimp_oc: bad arguments");
     if (prm->max_bisect <= 0 || prm->max_bisect > 1000)
         return set_error(GBS_EINVAL, "gbsimp_oc: max_bisect out of range");
@@ -617,7 +617,7 @@ int oc_check_args(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_oc
 
 extern "C" int gbsimp_oc_prepare(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const uint8_t *preserved,
                                  void *ws, size_t ws_bytes, void *stream) {
-    if (!ctx || nx <= 0 || ny <= 0 || nz <= 0 || !ws) return set_error(GBS_EINVAL, "gbsimp_oc_prepare: bad arguments");
+    if (!ctx || !grid_ok(nx, ny, nz) || !ws) return set_error(GBS_EINVAL, "gbsimp_oc_prepare: bad arguments");
     if (ws_bytes < oc_ws_bytes((int64_t)nx * ny * nz)) return set_error(GBS_EINVAL, "gbsimp_oc_prepare: workspace too small");
     return oc_prepare_impl(ctx, nx, ny, nz, rmin, preserved, ws, (cudaStream_t)stream);
 }

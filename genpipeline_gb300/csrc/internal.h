@@ -4,6 +4,12 @@
 #include "common.cuh"
 
 namespace gbs {
+// Grids the kernels accept: positive extents and DOF indices that fit in 32 bits
+// (3 (nx+1)(ny+1)(nz+1) < 2^31; node and DOF offsets are 32-bit in places).
+inline bool grid_ok(int nx, int ny, int nz) {
+    return nx > 0 && ny > 0 && nz > 0 && (int64_t)(nx + 1) * (ny + 1) * (nz + 1) < (1LL << 31) / 3;
+}
+
 int apply_f32(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
               const float *p, float *y, const uint8_t *mask, cudaStream_t st);
 int apply_f64(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,

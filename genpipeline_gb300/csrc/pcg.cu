@@ -1327,10 +1327,6 @@ static CsrWs csr_ws(void *ws, int64_t n) {
 
 using namespace gbs;
 
-static bool grid_ok(int nx, int ny, int nz) {
-    return nx > 0 && ny > 0 && nz > 0 && (int64_t)(nx + 1) * (ny + 1) * (nz + 1) < (1LL << 31) / 3;
-}
-
 extern "C" size_t gbsimp_pcg_ws_bytes(int nx, int ny, int nz) { return pcg_ws_bytes_impl(nx, ny, nz); }
 
 extern "C" size_t gbsimp_time_pcg_apply_ws_bytes(int nx, int ny, int nz) {

@@ -15,6 +15,8 @@
  *   element-local node a in the order (0,0,0),(1,0,0),(1,1,0),(0,1,0),(0,0,1),(1,0,1),
  *   (1,1,1),(0,1,1); element-local DOF 3a + c; Ke is row-major 24x24.
  * Dirichlet masks are one byte per node: bit c set = DOF 3n+c is fixed (held at 0).
+ * Grids: positive extents with fewer than 2^31 DOFs (3 (nx+1)(ny+1)(nz+1) < 2^31); the grid
+ * entry points return GBS_EINVAL for anything else.
  *
  * Return values: GBS_OK or one of the GBS_E* codes; gbsimp_last_error() gives the
  * message of the last failure on the calling thread.

@@ -87,6 +87,31 @@ def test_pcg_workspace_holds_the_one_kernel_partials():
             assert part >= 48 * nblk, (nx, ny, nz, wave)
 
 
+def test_grids_beyond_32_bit_dof_indices_are_refused():
+    """3 (nx+1)(ny+1)(nz+1) must stay below 2^31 for every grid entry point; the argument
+    checks run before the context is used (the placeholder context is never dereferenced)."""
+    lib = L.load()
+    ctx = C.c_void_p(16)
+    buf = C.c_void_p(256)
+    law = L.make_law("modified", 3.0)
+    big = (900, 900, 900)  # 3 * 901^3 > 2^31 DOFs
+    prm = L.OcParams()
+    calls = {
+        "gbsimp_apply_f32": lambda g: lib.gbsimp_apply_f32(ctx, *g, C.byref(law), buf, buf, buf, None, None),
+        "gbsimp_apply_f64": lambda g: lib.gbsimp_apply_f64(ctx, *g, C.byref(law), buf, buf, buf, None, None),
+        "gbsimp_sensitivity": lambda g: lib.gbsimp_sensitivity(ctx, *g, C.byref(law), buf, buf, buf, None, None, None, 0,
+                                                               None),
+        "gbsimp_filter_hs": lambda g: lib.gbsimp_filter_hs(ctx, *g, 1.5, buf, None),
+        "gbsimp_filter": lambda g: lib.gbsimp_filter(ctx, *g, 1.5, buf, buf, buf, 0, None),
+        "gbsimp_oc_prepare": lambda g: lib.gbsimp_oc_prepare(ctx, *g, 1.5, None, buf, 1 << 62, None),
+        "gbsimp_oc": lambda g: lib.gbsimp_oc(ctx, *g, 1.5, C.byref(prm), buf, buf, None, buf, buf, buf, 1 << 62, None),
+    }
+    for name, call in calls.items():
+        assert call(big) == L.GBS_EINVAL, name
+        assert b"bad arguments" in lib.gbsimp_last_error(), name
+        assert call((0, 4, 4)) == L.GBS_EINVAL, name
+
+
 def test_every_status_entry_point_rejects_null_arguments():
     """Every status-returning call, given a NULL context, zero sizes and NULL pointers, returns
     GBS_EINVAL with a message before touching the device (no GPU here)."""
