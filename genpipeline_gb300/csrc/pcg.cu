@@ -738,9 +738,14 @@ static int cg_publish(const gbsimp_ctx *ctx, int nx, int ny, int nz, const PcgWs
     return GBS_OK;
 }
 
-// Builds (or finds) the instantiated loop graph for this problem and buffer set.
-static int loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
-                      const uint8_t *mask, float *u, const PcgWs &w, cudaGraphExec_t *out) {
+// Builds (or finds) the instantiated loop graph for this problem and buffer set and launches
+// it on st, all under the cache's lock: another thread's eviction (the cache is emptied when
+// full) can then never destroy a graph between its lookup and its launch, and CUDA defers
+// the destruction of a graph that is still running. *built is false when no graph could be
+// built (the error is returned; the caller may run the host loop instead).
+static int launch_loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
+                             const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st, bool *built) {
+    *built = false;
     GraphCache *gc = (GraphCache *)ctx->graphs;
     if (!gc) return set_error(GBS_ECUDA, "no graph cache");
     const bool modal = use_modal(ctx, nz);
@@ -764,7 +769,8 @@ static int loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<f
     std::lock_guard<std::mutex> lock(gc->mu);
     auto it = gc->map.find(key);
     if (it != gc->map.end()) {
-        *out = it->second;
+        *built = true;
+        GBS_CUDA_TRY(cudaGraphLaunch(it->second, st));
         return GBS_OK;
     }
     if (gc->map.size() >= 64) {
@@ -828,7 +834,8 @@ static int loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<f
     cudaGraphDestroy(g);
     if (rc != GBS_OK) return rc;
     gc->map.emplace(key, exec);
-    *out = exec;
+    *built = true;
+    GBS_CUDA_TRY(cudaGraphLaunch(exec, st));
     return GBS_OK;
 }
 
@@ -926,9 +933,10 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
         // the grid cannot be co-resident here: use the graph loop
     }
     if (!prof && !h.done) {
-        cudaGraphExec_t exec = nullptr;
-        if (loop_graph(ctx, nx, ny, nz, law, x, mask, u, w, &exec) == GBS_OK) {
-            GBS_CUDA_TRY(cudaGraphLaunch(exec, st));
+        bool built = false;
+        const int lrc = launch_loop_graph(ctx, nx, ny, nz, law, x, mask, u, w, st, &built);
+        if (built) {
+            if (lrc) return lrc;  // the launch itself failed
             rc = cg_publish(ctx, nx, ny, nz, w, 1, st);
             if (rc) return rc;
             pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 2 : 1);
@@ -1633,10 +1641,9 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
         gbsimp_batch_item &it = items[i];
         SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
         PcgWs pw = pcg_ws(w.pcg, it.nx, it.ny, it.nz);
-        cudaGraphExec_t exec = nullptr;
-        int rc = loop_graph(ctx, it.nx, it.ny, it.nz, law, it.x, it.node_mask, w.d32, pw, &exec);
+        bool built = false;
+        int rc = launch_loop_graph(ctx, it.nx, it.ny, it.nz, law, it.x, it.node_mask, w.d32, pw, st, &built);
         if (rc) return rc;
-        GBS_CUDA_TRY(cudaGraphLaunch(exec, st));
         rc = cg_publish(ctx, it.nx, it.ny, it.nz, pw, 1, st);
         if (rc) return rc;
     }
