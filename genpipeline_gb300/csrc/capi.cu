@@ -87,12 +87,23 @@ static void ke_quadrature(double nu, double e0, double *ke) {
         }
 }
 
+namespace {
+// Owner of one thread's pinned buffer: freed when the thread exits (every use copies into it
+// and synchronises the stream before returning, so no copy is in flight by then).
+struct ThreadPinned {
+    void *p = nullptr;
+    ~ThreadPinned() {
+        if (p) cudaFreeHost(p);
+    }
+};
+}  // namespace
+
 void *thread_pinned() {
     // One small pinned buffer per host thread, so that threads sharing a context never
-    // share a staging buffer. It lives until the process exits.
-    static thread_local void *buf = nullptr;
-    if (!buf && cudaMallocHost(&buf, 4096) != cudaSuccess) buf = nullptr;
-    return buf;
+    // share a staging buffer.
+    static thread_local ThreadPinned buf;
+    if (!buf.p && cudaMallocHost(&buf.p, 4096) != cudaSuccess) buf.p = nullptr;
+    return buf.p;
 }
 
 static void install_ke(gbsimp_ctx *ctx, const double *ke) {
