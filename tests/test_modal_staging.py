@@ -9,6 +9,7 @@ starts on a 16-byte boundary and spans whole 16-byte groups; the destination lie
 RW-word raw buffer, on a 16-byte boundary; the group cut by the end of the vector goes to a
 whole group of the raw buffer. Every staged group is combined by some thread (nv <= groups
 per thread x 256) and the operand planes and element reads stay inside one RW-word slot.
+The x segments of modal_geom partition the planes (restated too).
 """
 import numpy as np
 import pytest
@@ -67,6 +68,41 @@ def test_staging_in_bounds_for_every_z_extent(cg):
                                   (17, 9, 37), (1, 1, 1)])
 def test_staging_in_bounds_for_test_and_bench_grids(grid, cg):
     _check(*grid, cg)
+
+
+def _segments(nx, ny, nz, sms, per_sm, edge):
+    """modal_geom's x segments: [xs, xe) per segment (restated)."""
+    f = NE - (nz + 2)
+    tiles = -(-(ny + 1) * (nz + 1) // f)
+    planes = nx if edge else nx + 1
+    nseg = max(1, min((sms * per_sm) // tiles, planes))
+    seglen, rem = planes // nseg, planes % nseg
+    out = []
+    for s in range(nseg):
+        xs = s * seglen + min(s, rem)
+        out.append((xs, min(xs + seglen + (1 if s < rem else 0), planes)))
+    return tiles, out
+
+
+@pytest.mark.parametrize("edge", [False, True])
+def test_segments_partition_the_planes(edge):
+    """Segments tile [0, planes) exactly, each non-empty, lengths within one plane of each
+    other; the launch (tiles x segments) fills at most one wave unless one plane's tiles
+    alone exceed it."""
+    rng = np.random.default_rng(2)
+    cases = [(64, 64, 64, 152, 2), (192, 96, 96, 152, 2), (3, 2, 446, 152, 1), (1, 300, 446, 152, 2)]
+    cases += [(int(rng.integers(1, 300)), int(rng.integers(1, 200)), int(rng.integers(1, 447)), 152,
+               int(rng.integers(1, 3))) for _ in range(300)]
+    for nx, ny, nz, sms, per_sm in cases:
+        tiles, segs = _segments(nx, ny, nz, sms, per_sm, edge)
+        planes = nx if edge else nx + 1
+        assert segs[0][0] == 0 and segs[-1][1] == planes
+        assert all(a[1] == b[0] for a, b in zip(segs, segs[1:]))
+        lens = [xe - xs for xs, xe in segs]
+        assert min(lens) >= 1 and max(lens) - min(lens) <= 1
+        assert tiles * len(segs) <= max(sms * per_sm, tiles)
+    tiles, segs = _segments(64, 64, 64, 152, 2, True)  # the 64^3 PCG launch: 10 tiles x 30 segments
+    assert (tiles, len(segs), sorted({b - a for a, b in segs})) == (10, 30, [2, 3])
 
 
 def test_random_grids():
