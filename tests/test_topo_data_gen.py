@@ -104,6 +104,18 @@ def test_generate_batches_records_and_failures(tmp_path, monkeypatch, method):
         assert rec["json"].endswith("_fem_results.json")
 
 
+def test_sensitivity_solve_schedule():
+    """(tol, max_iter) of each SIMP iteration's sensitivity solve, as SIMPSolverGPU.run sets
+    them (topology/simp_solver_gpu.py:94-100): 1e-4/200 for iterations 0-2, 1e-5/400 for 3-7,
+    1e-6/800 after."""
+    from genpipeline_gb300.topology.batch_simp import reference_schedule
+    from genpipeline_gb300.topology.simp_solver_gpu import SIMPSolverGPU
+
+    got = [reference_schedule(i) for i in (0, 2, 3, 7, 8, 79)]
+    assert got == [(1e-4, 200), (1e-4, 200), (1e-5, 400), (1e-5, 400), (1e-6, 800), (1e-6, 800)]
+    assert SIMPSolverGPU.tol_schedule is reference_schedule
+
+
 def test_generator_bcs_cover_every_geometry(tmp_path):
     from genpipeline_gb300 import bcs as B
 
