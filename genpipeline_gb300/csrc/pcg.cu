@@ -660,6 +660,9 @@ static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n,
         D.mask = itm.mask;
         D.ca = cg_args(itm.w, itm.u);
         block0 += D.nblk;
+        // the barrier writes two slots of three partial sums per CTA of the design
+        if (6 * (size_t)D.nblk > itm.w.partial_count)
+            return set_error(GBS_EINVAL, "fused PCG: a design's CTAs need more partial sums than its workspace holds");
     }
     unsigned long long wait_ns = 2000000000ull;  // 2 s per barrier wait
     Law<float> lw = law;
