@@ -5,9 +5,17 @@
 
 namespace gbs {
 // Grids the kernels accept: positive extents and DOF indices that fit in 32 bits
-// (3 (nx+1)(ny+1)(nz+1) < 2^31; node and DOF offsets are 32-bit in places).
+// (3 (nx+1)(ny+1)(nz+1) < 2^31; node and DOF offsets are 32-bit in places). Each extent is
+// widened before the +1 and bounded before the products, so no int or int64 arithmetic
+// here can wrap (INT_MAX + 1, or three extents near 2^30 multiplied together).
 inline bool grid_ok(int nx, int ny, int nz) {
-    return nx > 0 && ny > 0 && nz > 0 && (int64_t)(nx + 1) * (ny + 1) * (nz + 1) < (1LL << 31) / 3;
+    if (nx <= 0 || ny <= 0 || nz <= 0) return false;
+    const int64_t lim = (1LL << 31) / 3;
+    const int64_t a = (int64_t)nx + 1, b = (int64_t)ny + 1, c = (int64_t)nz + 1;
+    if (a >= lim || b >= lim || c >= lim) return false;
+    const int64_t ab = a * b;  // < 2^62: no overflow
+    if (ab >= lim) return false;
+    return ab * c < lim;       // ab < 2^30 and c < 2^30: no overflow
 }
 
 int apply_f32(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,

@@ -106,10 +106,18 @@ def test_grids_beyond_32_bit_dof_indices_are_refused():
         "gbsimp_oc_prepare": lambda g: lib.gbsimp_oc_prepare(ctx, *g, 1.5, None, buf, 1 << 62, None),
         "gbsimp_oc": lambda g: lib.gbsimp_oc(ctx, *g, 1.5, C.byref(prm), buf, buf, None, buf, buf, buf, 1 << 62, None),
     }
+    int_max = 2**31 - 1
+    # Extents whose +1 or whose products would wrap in 32- or 64-bit arithmetic, and the exact
+    # boundary: (461+1)(4680+1)(330+1) = 715,827,882 = floor(2^31 / 3) nodes, the first count
+    # refused (2*3*7*11 = 462, 31*151 = 4681, 331).
+    wrap = [(int_max, 1, 1), (1, int_max, 1), (1, 1, int_max), (int_max, int_max, int_max),
+            (2**30, 2**30, 2**30), (2**21, 2**21, 2**21), (461, 4680, 330), (330, 461, 4680)]
     for name, call in calls.items():
         assert call(big) == L.GBS_EINVAL, name
         assert b"bad arguments" in lib.gbsimp_last_error(), name
         assert call((0, 4, 4)) == L.GBS_EINVAL, name
+        for g in wrap:
+            assert call(g) == L.GBS_EINVAL, (name, g)
 
 
 def test_every_status_entry_point_rejects_null_arguments():
