@@ -2,7 +2,8 @@
 
 Each problem follows ``SIMPSolverGPU.run`` (topology/simp_solver_gpu.py:71-136): per
 iteration a warm-started sensitivity solve with the tolerance schedule (1e-4 / 200 PCG
-iterations for iterations 0-2, 1e-5 / 400 for 3-7, 1e-6 / 800 after), the floored law
+iterations for iterations 0-2, 1e-5 / 400 for 3-7, 1e-6 / 800 after; grids below 50,000
+DOFs to 1e-10, as the reference solves those directly), the floored law
 ``max(x, 1e-3)^penal``, the filtered sensitivity, the GPU OC variant, then a fresh compliance
 solve (1e-6 / 2000) whose displacement warm-starts the next iteration, and the early stop
 after three changes of compliance below 1%. The solves of all problems still running go
@@ -23,6 +24,12 @@ from .. import _lib as L
 from .. import bcs as B
 from ..batch import BatchFEM, FEMDesign
 from ..engine import Engine, get_engine, n_dof, n_elem
+
+
+# SIMPSolverGPU._solve factorises K directly below this many DOFs, ignoring the tolerance it
+# is given (simp_solver_gpu.py:581-588); such solves run to DIRECT_RTOL here.
+DIRECT_BELOW = 50000
+DIRECT_RTOL = 1e-10
 
 
 def reference_schedule(i: int):
@@ -74,13 +81,16 @@ class BatchSIMP:
             self._st.append(s)
 
     def _solve(self, idx: List[int], tol: float, max_iter: int, warm: bool):
-        """Batched solves of the given problems; returns {k: FEMDesign}."""
-        by_penal = {}
+        """Batched solves of the given problems; returns {k: FEMDesign}. Problems below
+        DIRECT_BELOW DOFs are solved to DIRECT_RTOL (the reference solves them directly)."""
+        groups = {}
         for k in idx:
-            by_penal.setdefault(self.cases[k].penal, []).append(k)
+            direct = n_dof(self.cases[k].grid) < DIRECT_BELOW
+            groups.setdefault((self.cases[k].penal, direct), []).append(k)
         out = {}
-        for penal, ks in by_penal.items():
-            bf = BatchFEM(self.eng, L.make_law("ref", penal), rtol=tol, max_iter=max_iter)
+        for (penal, direct), ks in groups.items():
+            rt, mi = (DIRECT_RTOL, 1000000) if direct else (tol, max_iter)
+            bf = BatchFEM(self.eng, L.make_law("ref", penal), rtol=rt, max_iter=mi)
             for k in ks:
                 s = self._st[k]
                 d = s["fem"]

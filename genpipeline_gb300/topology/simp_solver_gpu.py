@@ -14,7 +14,8 @@ Kept from the reference:
 Nothing is assembled. ``_assemble_K`` returns a matrix-free operator handle and ``_solve``
 runs the library's PCG on it. That PCG is FP32 inside an FP64 defect correction, to the
 reference's relative tolerance, warm-started from the previous displacement as ``_u_prev``
-is (:793).
+is (:793). Below 50,000 DOFs the reference factorises K directly whatever the tolerance
+(:581-588), so there the solve runs to 1e-10.
 """
 from __future__ import annotations
 
@@ -27,7 +28,7 @@ import torch
 from .. import _lib as L
 from .. import bcs as B
 from ..engine import Engine, get_engine, n_dof, n_elem
-from .batch_simp import reference_schedule
+from .batch_simp import DIRECT_BELOW, DIRECT_RTOL, reference_schedule
 
 
 @dataclass
@@ -85,6 +86,11 @@ class SIMPSolverGPU:
     _RESOURCE_CACHE = {}
     # (tol, max_iter) of the sensitivity solve per iteration (simp_solver_gpu.py:92-99)
     tol_schedule = staticmethod(reference_schedule)
+    # The reference's _solve factorises K directly (SuperLU) whenever the grid has fewer DOFs
+    # than this, whatever tolerance it is given (simp_solver_gpu.py:581-588): those solves run
+    # here to DIRECT_RTOL, so small grids follow the exact-solve trajectory as the reference's do.
+    DIRECT_BELOW = DIRECT_BELOW
+    DIRECT_RTOL = DIRECT_RTOL
 
     def __init__(self, nx: int = 32, ny: int = 8, nz: int = 8, penal: float = 3.0, rmin: float = 1.5,
                  boundary_conditions: dict | None = None, device: str = "cuda",
@@ -136,7 +142,10 @@ class SIMPSolverGPU:
                max_iter: int = 2000, x0: torch.Tensor | None = None) -> torch.Tensor:
         """u with K(x) u = f on the free DOFs to relative residual ``tol`` (at most
         ``max_iter`` PCG iterations; the best iterate is returned when the cap is hit, as the
-        reference's loop does)."""
+        reference's loop does). Grids below ``DIRECT_BELOW`` DOFs are solved to
+        ``DIRECT_RTOL`` instead, the accuracy of the reference's direct solve there."""
+        if n_dof(K.grid) < self.DIRECT_BELOW:
+            tol, max_iter = self.DIRECT_RTOL, 1000000
         ff = torch.as_tensor(f, device=self.device).reshape(-1).to(torch.float64).contiguous()
         u = torch.zeros_like(ff) if x0 is None else torch.as_tensor(x0, device=self.device).reshape(-1).to(
             torch.float64).clone()

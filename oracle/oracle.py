@@ -222,3 +222,76 @@ def simp_run(grid, ke, mat: Material, rmin, f, fixed, volfrac, n_iters, preserve
                              _u8(pres), float(volfrac), int(n_iters), float(tol), int(max_iter),
                              _d(x), _d(xp), _d(u), C.byref(c))
     return x, xp, u, c.value, tot
+
+
+def simp_gpu_run(grid, rmin, penal, f, fixed, volfrac, n_iters, preserved=None, x_init=None,
+                 schedule=None, direct_below=50000, exact_tol=1e-12, compliance_tol=1e-6,
+                 compliance_max_iter=2000, fp32_storage=False):
+    """``SIMPSolverGPU.run`` (genpipeline/topology/simp_solver_gpu.py:71-136) in FP64.
+
+    - x_init rescaled to the volume fraction and clamped to [1e-3, 1] (:80-84);
+      preserved elements set to 1 (:88-89);
+    - per iteration: the sensitivity solve warm-started from the last displacement with the
+      tolerance schedule (:92-99, ``schedule(i) -> (tol, max_iter)``), dc of the floored law
+      max(x, 1e-3)^penal (:753-794), the filter chain rule (:796-799), the GPU OC variant
+      (:801-841), then a cold compliance solve at the new design whose displacement
+      warm-starts the next iteration (:111, :747-751, ``_u_prev`` at :586-607);
+    - the early stop after three relative compliance changes below 1% (:113-125).
+    ``_solve`` solves directly (SuperLU) whenever the grid has fewer than 50,000 DOFs
+    (:581-588), whatever the tolerance: those solves run here to ``exact_tol``.
+    ``fp32_storage`` rounds dc, the filtered dc, x and xPhys to float32 where a
+    single-precision implementation stores them: the drift that storage alone causes.
+    Returns dict(xphys, history, last_compliance, iterations)."""
+    nx, ny, nz = grid
+    ne = nx * ny * nz
+    nd = 3 * (nx + 1) * (ny + 1) * (nz + 1)
+    mat = Material("ref", penal)
+    ke = ke_quadrature()
+    hs = filter_hs(grid, rmin)
+    f = _f64(f)
+    pres = None if preserved is None else np.asarray(preserved).reshape(-1).astype(bool)
+    if x_init is not None:
+        x = _f64(np.asarray(x_init).reshape(-1))
+        x = np.clip(x * (volfrac / max(x.mean(), 1e-6)), 1e-3, 1.0)
+    else:
+        x = np.full(ne, float(volfrac))
+    if pres is not None:
+        x[pres] = 1.0
+    xphys = x.copy()
+    direct = nd < direct_below
+    if schedule is None:
+        def schedule(i):
+            return (1e-4, 200) if i < 3 else (1e-5, 400) if i < 8 else (1e-6, 800)
+
+    def solve(u0, tol, max_iter):
+        if direct:
+            tol, max_iter = exact_tol, 1000000
+        u, _, _ = pcg(grid, ke, moduli(xphys, mat), f, fixed, u0=u0, tol=tol, max_iter=max_iter)
+        return u
+
+    u_prev = None
+    prev, changes, history = float("inf"), [], []
+    curr = float("nan")
+    it = 0
+    pmask = None if pres is None else pres.astype(np.uint8)
+    r32 = (lambda a: a.astype(np.float32).astype(np.float64)) if fp32_storage else (lambda a: a)
+    hs = r32(hs)
+    x, xphys = r32(x), r32(xphys)
+    for i in range(n_iters):
+        tol, max_iter = schedule(i)
+        u = solve(u_prev, tol, max_iter)
+        _, dc, _ = element_energy(grid, ke, xphys, u, mat)
+        dcf = r32(density_filter(grid, rmin, r32(dc), hs=hs, transpose=True))
+        x, xphys, _ = oc(grid, rmin, x, dcf, volfrac, preserved=pmask, hs=hs, variant=OC_GPU)
+        x, xphys = r32(x), r32(xphys)
+        uc = solve(None, compliance_tol, compliance_max_iter)
+        u_prev = uc
+        curr = float(f @ uc)
+        history.append(curr)
+        it = i + 1
+        if prev != float("inf"):
+            changes.append(abs(prev - curr) / (prev + 1e-10))
+        if len(changes) >= 3 and all(c < 0.01 for c in changes[-3:]):
+            break
+        prev = curr
+    return dict(xphys=xphys, history=np.array(history), last_compliance=curr, iterations=it)
