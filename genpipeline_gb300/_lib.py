@@ -57,8 +57,8 @@ class SolveOpts(C.Structure):
 
 class SolveStats(C.Structure):
     _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("outer", C.c_int32),
-                ("reserved", C.c_int32), ("relres", C.c_double), ("seconds", C.c_double),
-                ("apply_seconds", C.c_double), ("apply_launches", C.c_int32), ("reserved2", C.c_int32)]
+                ("inner_active", C.c_int32), ("relres", C.c_double), ("seconds", C.c_double),
+                ("apply_seconds", C.c_double), ("apply_launches", C.c_int32), ("inner_iters", C.c_int32)]
 
     def as_dict(self):
         return {"status": int(self.status), "status_name": STATUS_NAMES.get(int(self.status), "?"),

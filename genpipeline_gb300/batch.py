@@ -48,14 +48,17 @@ class FEMDesign:
 
 
 class BatchFEM:
-    """Runs gbsimp_batch_round over a changing set of designs."""
+    """Runs gbsimp_batch_round over a changing set of designs. ``round_iters`` > 0 bounds the
+    inner PCG iterations of one round (a solve still running is paused and resumes in the
+    next round), so that a serving loop regains control every few milliseconds."""
 
     def __init__(self, engine: Optional[Engine] = None, law: Optional[L.Law] = None, rtol: float = 1e-8,
-                 inner_rtol: float = 1e-4, max_iter: int = 200000, max_outer: int = 30, fused: bool = True):
+                 inner_rtol: float = 1e-4, max_iter: int = 200000, max_outer: int = 30, fused: bool = True,
+                 round_iters: int = 0):
         self.eng = engine or get_engine()
         self.law = law or L.make_law("modified", 3.0)
         self.opts = Engine.opts(rtol=rtol, inner_rtol=inner_rtol, max_iter=max_iter, max_outer=max_outer,
-                                fused=int(fused))
+                                fused=int(fused), check_every=int(round_iters))
         self.items: List[FEMDesign] = []
         self._structs = None
 
@@ -104,11 +107,22 @@ class BatchFEM:
         self.items = keep
         return done
 
+    def remove(self, d: FEMDesign) -> bool:
+        """Drops a design between rounds (a cancelled request); its inner solve, paused or not,
+        is abandoned. Returns False when it is not in the batch."""
+        for i, e in enumerate(self.items):
+            if e is d:
+                del self.items[i]
+                return True
+        return False
+
     def solve_all(self, designs: List[FEMDesign]) -> List[FEMDesign]:
         for d in designs:
             self.add(d)
         out = []
-        for _ in range(int(self.opts.max_outer) + 2):
+        # each item ends within max_outer FP64 rounds; a round budget adds rounds per correction
+        per = 1 if self.opts.check_every <= 0 else 1 + int(self.opts.max_iter) // int(self.opts.check_every)
+        for _ in range((int(self.opts.max_outer) + 2) * per):
             out += self.round()
             if not self.items:
                 break
@@ -122,11 +136,12 @@ class SolveQueue:
     BatchFEM, with the queue kept by the library."""
 
     def __init__(self, engine: Optional[Engine] = None, law: Optional[L.Law] = None, rtol: float = 1e-8,
-                 inner_rtol: float = 1e-4, max_iter: int = 200000, max_outer: int = 30, fused: bool = True):
+                 inner_rtol: float = 1e-4, max_iter: int = 200000, max_outer: int = 30, fused: bool = True,
+                 round_iters: int = 0):
         self.eng = engine or get_engine()
         self.law = law or L.make_law("modified", 3.0)
         self.opts = Engine.opts(rtol=rtol, inner_rtol=inner_rtol, max_iter=max_iter, max_outer=max_outer,
-                                fused=int(fused))
+                                fused=int(fused), check_every=int(round_iters))
         h = C.c_void_p()
         L.check(self.eng.lib.gbsimp_queue_create(self.eng.ctx, C.byref(self.law), C.byref(self.opts), C.byref(h)))
         self._q = h

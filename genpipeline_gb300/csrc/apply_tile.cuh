@@ -53,6 +53,8 @@ struct PcgScalars {
     unsigned bar_count, bar_gen;  // grid barrier of the persistent kernel
     int trips;        // WHILE-loop trips run by the device-driven loop
     int max_trips;    // hard cap on those trips (the loop always ends)
+    int pause_trips;  // > 0: the loop stops after this many trips without ending the solve
+                      // (batched rounds with an iteration budget resume it in the next round)
     int freeze;       // 1 = kernels leave the scalars as they are (timing of one pass)
     float rr_stop;    // one-kernel PCG: (tol ||D b||)^2 in FP32, the stop test on r.r
     CgState st[2];    // one-kernel PCG: the state by launch parity

@@ -362,6 +362,7 @@ __global__ void __launch_bounds__(256) pcg_update_kernel(int64_t nd, const float
 // alpha).
 __global__ void pcg_finalize_kernel(int64_t nd, const float *p0, const float *p1, float *xu, const PcgScalars *sc,
                                     int lazy) {
+    if (!sc->done) return;  // paused by a batched round's budget: the next round resumes it
     const int st = sc->status;
     const int it = sc->iter;
     const bool zero = sc->bnorm == 0.0;
@@ -516,7 +517,7 @@ struct FusedTable {
 template <int NT, int EPT, int MAXV>
 __global__ void __launch_bounds__(NT, 2)
     pcg_fused_kernel(const __grid_constant__ FusedTable T, Law<float> law, const ModalK km,
-                     unsigned long long wait_ns) {
+                     unsigned long long wait_ns, int budget) {
     extern __shared__ float4 smem4[];
     __shared__ float2 sred[3 * 32];
     int di = 0;
@@ -538,7 +539,10 @@ __global__ void __launch_bounds__(NT, 2)
     const float rr_stop = (float)(stop * stop);
     const int max_iter = vsc->max_iter;
     unsigned target = 0;
-    while (!done) {
+    // budget > 0: at most `budget` iterations in this launch; the state is written back with
+    // `done` clear and the next launch resumes from it (iteration, scalars, buffer parity)
+    const int it_end = budget > 0 ? it + budget : 0x7fffffff;
+    while (!done && it < it_end) {
         const int c = it & 1, nc = c ^ 1;
         const CgPass cp{alpha.hi, beta.hi, ca.r[c], ca.w[c], ca.s[nc], ca.dinv, ca.r[nc], ca.s[c], ca.p, ca.xu, nullptr, ca.sc, 1};
         float sums[3];
@@ -564,7 +568,7 @@ __global__ void __launch_bounds__(NT, 2)
     }
     if (bid == 0 && threadIdx.x == 0) {
         sc->iter = it;
-        sc->done = 1;
+        sc->done = done;
         sc->status = status;
         sc->rz = df_value(gamma_i);
         sc->rr = df_value(rr);
@@ -583,12 +587,19 @@ struct FusedItem {
     PcgWs w;
 };
 
-// Runs the remaining PCG iterations of up to kMaxFused initialised designs in one
-// cooperative launch. The CTAs of the GPU are shared in proportion to the designs' element
-// counts (at least one segment of flat tiles each). Returns GBS_EINVAL when the designs cannot
-// all be resident at once (the caller then iterates them with the graph loop).
-static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n, const Law<float> &law,
-                           cudaStream_t st) {
+// One cooperative launch of the persistent kernel over up to kMaxFused designs.
+struct FusedPlan {
+    void *kern;
+    size_t smem;
+    unsigned blocks;
+    FusedTable T;
+};
+
+// Plans the launch of up to kMaxFused initialised designs: the CTAs of the GPU are shared in
+// proportion to the designs' element counts (at least one segment of flat tiles each).
+// Returns GBS_EINVAL when the designs cannot all be resident at once (the caller then
+// iterates them with the graph loop, or splits them over several launches). Host only.
+static int fused_plan(const gbsimp_ctx *ctx, const FusedItem *items, int n, FusedPlan *plan) {
     if (n <= 0 || n > kMaxFused || !ctx->modal_ok) return GBS_EINVAL;
     bool small = true;
     int max_nz = 0;
@@ -643,7 +654,7 @@ static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n,
         nseg[j] -= 1;
         used -= tiles[j];
     }
-    FusedTable T;
+    FusedTable &T = plan->T;
     memset(&T, 0, sizeof T);
     T.n = n;
     int block0 = 0;
@@ -664,11 +675,27 @@ static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n,
         if (6 * (size_t)D.nblk > itm.w.partial_count)
             return set_error(GBS_EINVAL, "fused PCG: a design's CTAs need more partial sums than its workspace holds");
     }
+    plan->kern = kern;
+    plan->smem = smem;
+    plan->blocks = (unsigned)block0;
+    return GBS_OK;
+}
+
+// Runs up to `budget` further PCG iterations (0: all that remain) of up to kMaxFused
+// initialised designs in one cooperative launch (plan: fused_plan). A design that reaches the
+// budget keeps `done` clear and resumes in the next launch; its barrier counter restarts here.
+static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n, const Law<float> &law,
+                           cudaStream_t st, int budget = 0) {
+    FusedPlan P;
+    int rc = fused_plan(ctx, items, n, &P);
+    if (rc) return rc;
+    for (int i = 0; i < n; ++i)
+        GBS_CUDA_TRY(cudaMemsetAsync(&items[i].w.sc->bar_count, 0, sizeof(unsigned), st));
     unsigned long long wait_ns = 2000000000ull;  // 2 s per barrier wait
     Law<float> lw = law;
     ModalK km = ctx->km;
-    void *args[] = {&T, &lw, &km, &wait_ns};
-    const cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3((unsigned)block0), dim3(kModalNT), args, smem, st);
+    void *args[] = {&P.T, &lw, &km, &wait_ns, &budget};
+    const cudaError_t e = cudaLaunchCooperativeKernel(P.kern, dim3(P.blocks), dim3(kModalNT), args, P.smem, st);
     if (e != cudaSuccess) {
         cudaGetLastError();  // a refused launch must not surface at the next launch check
         return set_error(GBS_EINVAL, "cooperative launch refused: %s", cudaGetErrorString(e));
@@ -699,7 +726,17 @@ __global__ void pcg_loop_cond_kernel(cudaGraphConditionalHandle h, PcgScalars *s
         sc->status = GBS_ETIMEOUT;
         stop = true;
     }
+    // an iteration budget pauses the solve at a trip boundary (launch phase 5 done, so the
+    // next launch of the same solve is phase 0 again); `done` stays clear
+    if (!stop && sc->pause_trips > 0 && trips >= sc->pause_trips) stop = true;
     cudaGraphSetConditional(h, stop ? 0u : 1u);
+}
+
+// Before a graph-loop launch of a batched round: restarts the trip count (the cap max_trips
+// then bounds every launch) and pauses after `trips` trips (0 = run to the end).
+__global__ void pcg_set_pause_kernel(PcgScalars *sc, int trips) {
+    sc->trips = 0;
+    sc->pause_trips = trips;
 }
 
 struct GraphCache {
@@ -1559,18 +1596,25 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
     const Law<float> law = make_law<float>(*glaw);
     const int max_outer = o->max_outer > 0 ? o->max_outer : 20;
     const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-4;
-    std::vector<int> act;
+    // iteration budget of the inner PCGs in this round (0: each runs to its tolerance)
+    const int budget = o->check_every > 0 ? o->check_every : 0;
+    // act: every active item; res: those between inner solves, which get an FP64 residual
+    // (the others resume their paused inner PCG)
+    std::vector<int> act, res;
     for (int i = 0; i < n; ++i)
-        if (items[i].state == 0) act.push_back(i);
+        if (items[i].state == 0) {
+            act.push_back(i);
+            if (items[i].stats.inner_active == 0) res.push_back(i);
+        }
     if (act.empty()) return GBS_OK;
-    // ---- FP64 residuals of every active item, one sync ------------------------------------
+    // ---- FP64 residuals of the items between inner solves, one sync -------------------------
     void *hp = thread_pinned();
     if (!hp) return set_error(GBS_ECUDA, "no pinned staging buffer");
     const size_t per = sizeof(OuterScalars);
-    for (size_t k = 0; k < act.size(); k += 4096 / per) {
-        const size_t m = std::min(act.size() - k, (size_t)(4096 / per));
+    for (size_t k = 0; k < res.size(); k += 4096 / per) {
+        const size_t m = std::min(res.size() - k, (size_t)(4096 / per));
         for (size_t j = 0; j < m; ++j) {
-            gbsimp_batch_item &it = items[act[k + j]];
+            gbsimp_batch_item &it = items[res[k + j]];
             const int64_t nd = n_dof_of(it.nx, it.ny, it.nz);
             SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
             if (it.stats.outer == 0) GBS_CUDA_TRY(cudaMemsetAsync(w.os, 0, sizeof(OuterScalars), st));
@@ -1584,7 +1628,7 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
         }
         GBS_CUDA_TRY(cudaStreamSynchronize(st));
         for (size_t j = 0; j < m; ++j) {
-            gbsimp_batch_item &it = items[act[k + j]];
+            gbsimp_batch_item &it = items[res[k + j]];
             OuterScalars h;
             memcpy(&h, (char *)hp + j * per, per);
             gbsimp_solve_stats &s = it.stats;
@@ -1609,12 +1653,11 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
             }
         }
     }
-    // ---- inner FP32 PCG of the items still above rtol ---------------------------------------
-    std::vector<int> inn;
-    for (int i : act)
-        if (items[i].state == 0) inn.push_back(i);
-    if (inn.empty()) return GBS_OK;
-    for (int i : inn) {
+    // ---- new inner FP32 PCGs of the items still above rtol ------------------------------------
+    std::vector<int> fresh;
+    for (int i : res)
+        if (items[i].state == 0) fresh.push_back(i);
+    for (int i : fresh) {
         gbsimp_batch_item &it = items[i];
         const int64_t nd = n_dof_of(it.nx, it.ny, it.nz);
         SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
@@ -1627,30 +1670,85 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
                            o->max_iter - it.stats.iterations, pw, st, SETUP_X0_ZERO);
         if (rc) return rc;
     }
-    // persistent batched launches (fall back to each item's graph loop)
-    std::vector<int> pending;
-    for (size_t k = 0; k < inn.size(); k += kMaxFused) {
-        const size_t m = std::min(inn.size() - k, (size_t)kMaxFused);
+    // ---- run the inner PCGs: paused persistent solves, then the new ones ---------------------
+    // A paused solve resumes in the form it started in (the persistent kernel and the graph loop
+    // keep their scalars differently). New solves are packed greedily into persistent launches
+    // of designs that are resident together; one that fits no launch runs its own graph loop.
+    auto fitem = [&](int i) {
+        gbsimp_batch_item &it = items[i];
+        SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
+        return FusedItem{it.nx, it.ny, it.nz, it.x, it.node_mask, w.d32, pcg_ws(w.pcg, it.nx, it.ny, it.nz)};
+    };
+    auto fits = [&](const std::vector<int> &c) {
+        if (c.empty() || c.size() > (size_t)kMaxFused) return false;
         FusedItem fi[kMaxFused];
-        for (size_t j = 0; j < m; ++j) {
-            gbsimp_batch_item &it = items[inn[k + j]];
-            SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
-            fi[j] = FusedItem{it.nx, it.ny, it.nz, it.x, it.node_mask, w.d32, pcg_ws(w.pcg, it.nx, it.ny, it.nz)};
-        }
-        if (!o->fused || pcg_fused_batch(ctx, fi, (int)m, law, st) != GBS_OK)
-            for (size_t j = 0; j < m; ++j) pending.push_back(inn[k + j]);
+        for (size_t j = 0; j < c.size(); ++j) fi[j] = fitem(c[j]);
+        FusedPlan P;
+        return fused_plan(ctx, fi, (int)c.size(), &P) == GBS_OK;
+    };
+    std::vector<int> order, graph_items;
+    for (int i : act)
+        if (items[i].state == 0 && items[i].stats.inner_active == 1) order.push_back(i);
+    for (int i : act)
+        if (items[i].state == 0 && items[i].stats.inner_active == 2) graph_items.push_back(i);
+    for (int i : fresh) {
+        if (o->fused && ctx->modal_ok) order.push_back(i);
+        else graph_items.push_back(i);
     }
-    for (int i : pending) {
+    std::vector<std::vector<int>> chunks;
+    std::vector<int> cur;
+    for (int i : order) {
+        cur.push_back(i);
+        if (fits(cur)) continue;
+        cur.pop_back();
+        if (!cur.empty()) chunks.push_back(cur);
+        cur.assign(1, i);
+        if (fits(cur)) continue;
+        cur.clear();
+        if (items[i].stats.inner_active == 1) {  // cannot happen: it ran in such a launch before
+            items[i].stats.status = set_error(GBS_EINVAL, "gbsimp_batch: a paused solve no longer fits a launch");
+            items[i].state = 2;
+        } else {
+            graph_items.push_back(i);
+        }
+    }
+    if (!cur.empty()) chunks.push_back(cur);
+    std::vector<int> fused_items;
+    for (const auto &c : chunks) {
+        FusedItem fi[kMaxFused];
+        for (size_t j = 0; j < c.size(); ++j) fi[j] = fitem(c[j]);
+        if (pcg_fused_batch(ctx, fi, (int)c.size(), law, st, budget) == GBS_OK) {
+            fused_items.insert(fused_items.end(), c.begin(), c.end());
+            continue;
+        }
+        for (int i : c) {  // launch refused
+            if (items[i].stats.inner_active == 1) {
+                items[i].stats.status = GBS_EINVAL;
+                items[i].state = 2;
+            } else {
+                graph_items.push_back(i);
+            }
+        }
+    }
+    const int pause_trips = budget > 0 ? (budget + kLoopUnroll - 1) / kLoopUnroll : 0;
+    for (int i : graph_items) {
         gbsimp_batch_item &it = items[i];
         SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
         PcgWs pw = pcg_ws(w.pcg, it.nx, it.ny, it.nz);
+        pcg_set_pause_kernel<<<1, 1, 0, st>>>(pw.sc, pause_trips);
+        GBS_LAUNCH_CHECK("pcg_set_pause_kernel");
         bool built = false;
         int rc = launch_loop_graph(ctx, it.nx, it.ny, it.nz, law, it.x, it.node_mask, w.d32, pw, st, &built);
         if (rc) return rc;
         rc = cg_publish(ctx, it.nx, it.ny, it.nz, pw, 1, st);
         if (rc) return rc;
     }
-    // finalize, read every item's PCG scalars (one sync), correct u
+    std::vector<int> inn(fused_items);
+    inn.insert(inn.end(), graph_items.begin(), graph_items.end());
+    if (inn.empty()) return GBS_OK;
+    const size_t n_fused = fused_items.size();
+    // finalize the solves that ended (a paused one is left as it is), read every item's PCG
+    // scalars (one sync), correct u of the ended ones
     const size_t ps = sizeof(PcgScalars);
     for (size_t k = 0; k < inn.size(); k += 4096 / ps) {
         const size_t m = std::min(inn.size() - k, (size_t)(4096 / ps));
@@ -1659,8 +1757,8 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
             const int64_t nd = n_dof_of(it.nx, it.ny, it.nz);
             SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
             PcgWs pw = pcg_ws(w.pcg, it.nx, it.ny, it.nz);
-            // one-kernel graph loop (the pending items): x may owe a half step; persistent: complete
-            const bool graph_loop = std::find(pending.begin(), pending.end(), inn[k + j]) != pending.end();
+            // one-kernel graph loop: x may owe a half step; persistent: complete
+            const bool graph_loop = k + j >= n_fused;
             pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, pw.p0, pw.p1, w.d32, pw.sc,
                                                                     use_modal(ctx, it.nz) ? (graph_loop ? 2 : 0) : 1);
             GBS_LAUNCH_CHECK("pcg_finalize_kernel");
@@ -1669,11 +1767,18 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
         GBS_CUDA_TRY(cudaStreamSynchronize(st));
         for (size_t j = 0; j < m; ++j) {
             gbsimp_batch_item &it = items[inn[k + j]];
+            const bool graph_loop = k + j >= n_fused;
             PcgScalars h;
             memcpy(&h, (char *)hp + j * ps, ps);
-            if (std::find(pending.begin(), pending.end(), inn[k + j]) != pending.end())
-                count_launches(h.trips * launches_per_trip(ctx, it.nz));
-            it.stats.iterations += h.iter;
+            if (graph_loop) count_launches(h.trips * launches_per_trip(ctx, it.nz));
+            it.stats.iterations += h.iter - it.stats.inner_iters;
+            if (!h.done) {  // paused by the budget: resumes next round, in the same form
+                it.stats.inner_iters = h.iter;
+                it.stats.inner_active = graph_loop ? 2 : 1;
+                continue;
+            }
+            it.stats.inner_iters = 0;
+            it.stats.inner_active = 0;
             if (h.status == GBS_EBREAKDOWN || h.status == GBS_ENONFINITE || h.status == GBS_ETIMEOUT) {
                 it.stats.status = h.status;
                 if (h.iter == 0 || h.status == GBS_ETIMEOUT) {
@@ -1703,6 +1808,8 @@ static int check_batch(gbsimp_ctx *ctx, gbsimp_batch_item *items, int n, const g
             return set_error(GBS_EINVAL, "gbsimp_batch: item %d has bad arguments", i);
         if (it.ws_bytes < solve_ws_bytes_impl(it.nx, it.ny, it.nz))
             return set_error(GBS_EINVAL, "gbsimp_batch: item %d workspace too small", i);
+        if (it.stats.inner_active < 0 || it.stats.inner_active > 2 || it.stats.inner_iters < 0)
+            return set_error(GBS_EINVAL, "gbsimp_batch: item %d has library-owned stats fields set (zero its stats)", i);
     }
     return GBS_OK;
 }
@@ -1718,8 +1825,11 @@ extern "C" int gbsimp_batch_solve(gbsimp_ctx *ctx, gbsimp_batch_item *items, int
                                   const gbsimp_solve_opts *opts, void *stream) {
     int rc = check_batch(ctx, items, n, law, opts);
     if (rc) return rc;
-    const int max_rounds = (opts->max_outer > 0 ? opts->max_outer : 20) + 2;
-    for (int r = 0; r < max_rounds; ++r) {
+    // every item ends within max_outer FP64 rounds; a round budget splits each inner solve over
+    // at most max_iter / budget + 1 rounds
+    int64_t max_rounds = (opts->max_outer > 0 ? opts->max_outer : 20) + 2;
+    if (opts->check_every > 0) max_rounds *= 1 + (int64_t)(opts->max_iter > 0 ? opts->max_iter : 0) / opts->check_every;
+    for (int64_t r = 0; r < max_rounds; ++r) {
         bool any = false;
         for (int i = 0; i < n; ++i) any = any || items[i].state == 0;
         if (!any) break;

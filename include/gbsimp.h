@@ -71,7 +71,11 @@ typedef struct gbsimp_solve_opts {
     int32_t max_iter;     /* cap on the total FP32 PCG iterations */
     int32_t max_outer;    /* cap on FP64 defect corrections (gbsimp_solve, batched rounds) */
     int32_t check_every;  /* iterations between the host's checks where the host drives the
-                             loop (profile, the CSR PCG); 0 = auto */
+                             loop (profile, the CSR PCG); 0 = auto. Batched rounds: the inner
+                             PCG iterations one round may run per item (rounded up to whole
+                             graph-loop trips of 12 there), after which the round returns and the
+                             paused solves resume in the next one; 0 = every inner PCG runs to
+                             its tolerance within the round */
     int32_t fused;        /* 1 = persistent fused PCG kernel, 0 = graph loop, one launch per iteration */
     int32_t profile;      /* 1 = time every PCG apply launch with CUDA events (stats) */
     int32_t reserved;
@@ -81,12 +85,14 @@ typedef struct gbsimp_solve_stats {
     int32_t status;       /* GBS_OK, GBS_ENOTCONV, GBS_EBREAKDOWN, GBS_ENONFINITE, GBS_ETIMEOUT */
     int32_t iterations;   /* FP32 PCG iterations (all outer corrections together) */
     int32_t outer;        /* FP64 residual evaluations */
-    int32_t reserved;
+    int32_t inner_active; /* batched rounds (library-owned, start at 0): 1 or 2 while an inner
+                             PCG is paused by the round budget (persistent kernel / graph loop) */
     double relres;        /* last ||D(f - K u)|| / ||D f|| */
     double seconds;       /* host wall time of the call */
     double apply_seconds; /* device time of the PCG apply launches (opts->profile only) */
     int32_t apply_launches;
-    int32_t reserved2;
+    int32_t inner_iters;  /* batched rounds (library-owned): iterations of the paused inner PCG
+                             already counted in `iterations` */
 } gbsimp_solve_stats;
 
 typedef struct gbsimp_ctx gbsimp_ctx;
@@ -97,7 +103,9 @@ int gbsimp_abi_version(void);
 uint64_t gbsimp_launch_count(void);
 const char *gbsimp_last_error(void);
 /* Creates a context bound to the current CUDA device, holding the quadrature element
- * stiffness of (nu = 0.3, E = 1). No device memory is allocated. */
+ * stiffness of (nu = 0.3, E = 1). No device memory is allocated. A context (and the CUDA
+ * graphs it caches) belongs to the device's primary context: destroy it before any
+ * cudaDeviceReset and create a new one afterwards. */
 int gbsimp_create(gbsimp_ctx **out);
 int gbsimp_destroy(gbsimp_ctx *ctx);
 /* Unit-cube trilinear hexahedron by 2x2x2 Gauss quadrature of B^T D B (host, FP64). The
@@ -178,7 +186,10 @@ int gbsimp_oc(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin,
  * device looks up that array's device address (call it with the context's device current);
  * make that first call before any stream capture. All calls share the one array and each
  * call re-initialises what it reads: calls that overlap on the GPU (other streams, other
- * threads) race and must not be issued. */
+ * threads) race and must not be issued. The final multiplier and bisection step count stay in
+ * that array, which gbsimp_oc_result cannot reach: they are not available from this entry
+ * point. The array's address is cached per device for the life of the process, so, like
+ * every context of this library, it must not be used across a cudaDeviceReset. */
 #define GBSIMP_OC_NOALLOC_MAX_ELEMENTS 2097152
 int gbsimp_oc_noalloc(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin,
                       const gbsimp_oc_params *prm, const float *x, const float *dc,
@@ -239,11 +250,14 @@ typedef struct gbsimp_batch_item {
 /* One round of the FP64 defect correction for every active item: FP64 residuals (one sync
  * for all), then the FP32 PCG of every item still above rtol, then the FP64 corrections.
  * With opts->fused the PCGs run as cooperative launches of a persistent kernel, up to 24
- * items per launch, each item on its own share of the SMs with its own grid barrier and
- * scalars, converging independently. A group whose items cannot all be resident at once,
- * or any item when opts->fused is 0, runs its own device-driven graph loop instead, enqueued
- * on the same stream. Items may be added (state 0) or dropped between rounds: the serving loop's
- * continuous batching. Replaces one gbsimp_solve per design (the reference's one solve per
+ * items per launch (packed greedily from the items that are resident together), each item on
+ * its own share of the SMs with its own grid barrier and scalars, converging independently.
+ * An item that fits no such launch, or any item when opts->fused is 0, runs its own
+ * device-driven graph loop instead, enqueued on the same stream. With opts->check_every > 0 a
+ * round runs at most that many inner iterations per item: an inner PCG still running then is
+ * paused (stats.inner_active) and continues in the next round, so a round lasts a bounded time
+ * whatever the grid sizes. Items may be added (state 0) or dropped between rounds: the serving
+ * loop's continuous batching. Replaces one gbsimp_solve per design (the reference's one solve per
  * GPUVoxelFEM.solve, gpu_fem_solver.py:76-133, fed by evaluate_batch's thread pool,
  * voxel_fem.py:559-611). Synchronises the stream. */
 int gbsimp_batch_round(gbsimp_ctx *ctx, gbsimp_batch_item *items, int n, const gbsimp_law *law,

@@ -30,11 +30,14 @@ def _designs():
     return out
 
 
-@pytest.mark.parametrize("fused", [True, False])
-def test_batch_equals_single_solves(fused):
+@pytest.mark.parametrize("fused,round_iters", [(True, 0), (False, 0), (True, 7), (False, 30)])
+def test_batch_equals_single_solves(fused, round_iters):
+    """Whole inner solves per round, and rounds of 7 (persistent kernel) or 30 (graph loop, two
+    12-iteration trips, then three) inner iterations after which each solve is paused and
+    resumed in the next round."""
     eng = Engine()
     single = solve_plain(_designs(), eng)
-    batch = BatchFEM(eng, fused=fused).solve_all(_designs())
+    batch = BatchFEM(eng, fused=fused, round_iters=round_iters).solve_all(_designs())
     assert len(batch) == len(single)
     by_grid = {d.grid: d for d in batch}
     for s in single:

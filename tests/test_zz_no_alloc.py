@@ -63,6 +63,37 @@ def test_noalloc_oc_matches_oc_on_consecutive_calls():
         np.testing.assert_allclose(xp.cpu().numpy(), xp_ref.cpu().numpy(), rtol=RTOL, atol=ATOL)
 
 
+def test_noalloc_oc_allocates_no_device_memory():
+    """After one call per variant (which loads the array's address and the kernels), further
+    calls leave the device's free memory unchanged: the scratch is the library's own array."""
+    eng = Engine()
+    grid, rmin, vf = (48, 24, 20), 2.0, 0.3
+    x, dc, pres = _case(grid, 5, True)
+    xn, xp = torch.empty_like(x), torch.empty_like(x)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def call(variant, p):
+        prm = L.make_oc(vf, variant)
+        L.check(eng.lib.gbsimp_oc_noalloc(eng.ctx, *grid, float(rmin), C.byref(prm), _ptr(x), _ptr(dc), _ptr(p),
+                                          _ptr(xn), _ptr(xp), stream))
+
+    for variant in (L.OC_CPU, L.OC_GPU):
+        for p in (pres, None):
+            call(variant, p)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        for variant in (L.OC_CPU, L.OC_GPU):
+            for p in (pres, None):
+                call(variant, p)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    xn_ref, xp_ref = eng.oc(grid, rmin, vf, x, dc, None, L.OC_GPU)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(xn.cpu().numpy(), xn_ref.cpu().numpy(), rtol=RTOL, atol=ATOL)
+    np.testing.assert_allclose(xp.cpu().numpy(), xp_ref.cpu().numpy(), rtol=RTOL, atol=ATOL)
+
+
 def test_noalloc_oc_rejects_grids_above_its_limit():
     eng = Engine()
     x, dc, xn, xp = (torch.zeros(8, device="cuda") for _ in range(4))  # never touched: rejected first
