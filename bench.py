@@ -63,8 +63,12 @@ def _args():
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["apply"], default="simp64",
                     help="simp64 (the bench line), c0, c4, serve, or apply (the bare stiffness apply)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-steps", type=int, default=1)
-    ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--cpu-sample-steps", type=int, default=3,
+                    help="OC iterations of the CPU oracle sample (the line reports their median)")
+    ap.add_argument("--serve-requests", type=int, default=2000, help="requests of --workload serve")
+    ap.add_argument("--line-serve-requests", type=int, default=300,
+                    help="requests of the serving stream inside the default line (0: skip it)")
+    ap.add_argument("--no-c4", action="store_true", help="skip the 192x96x96 kernel timings of the default line")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched FEM (served vs plain) measurement")
     ap.add_argument("--no-rows", action="store_true",
                     help="skip the evaluator / STL / generator measurements")
@@ -80,6 +84,13 @@ def _wl(a):
            "dofs": 3 * (g[0] + 1) * (g[1] + 1) * (g[2] + 1), "rmin": w["rmin"], "volfrac": w["volfrac"],
            "load": w["load_text"], **COMMON}
     return w, g, cfg
+
+
+def _line_keys(world: int) -> dict:
+    """Config keys both arms report (their config dicts differ only in `solver`)."""
+    return {"l2": "the GPU arm flushes L2 (256 MB write) before every timed step; inside a step the PCG "
+                  "vectors stay in L2 when they fit (64^3: ~36 MB)",
+            "parallelism": f"replicas x{world}" if world > 1 else "one replica"}
 
 
 def _spec(w):
@@ -434,37 +445,121 @@ def run_apply(a):
     print(json.dumps(line), flush=True)
 
 
-def run_serve(a):
-    """Serving stream: Poisson arrivals at 200/s, edge U{24,32,48,64,96}, three load cases,
-    ~10% repeated designs; continuous batching with admission by free HBM."""
-    import torch
+SERVE_ROUND_ITERS = 256  # inner PCG iterations per round: admissions every few milliseconds
+
+
+def measure_serving(n_requests: int, n_plain: int, clocks=None):
+    """The serving stream: Poisson arrivals at 200/s, edge U{24,32,48,64,96}, three load cases,
+    ~10% repeated designs, densities drawn by the client before the clock starts (they arrive
+    with the requests); continuous batching (24 slots, rounds of SERVE_ROUND_ITERS inner
+    iterations) with admission by free HBM. Beside it the plain form: one slot, one solve at a
+    time, on the first `n_plain` of the same requests with the same payloads, all queued at
+    t = 0 (its throughput is not limited by arrivals)."""
+    import numpy as np
 
     from genpipeline_gb300 import _lib as L
     from genpipeline_gb300.serve import FEMServer, attach_payloads, request_stream
 
     lib = L.load()
-    warm = FEMServer(max_slots=8)
+    warm = FEMServer(max_slots=8, round_iters=SERVE_ROUND_ITERS)
     warm.run(attach_payloads(request_stream(40, rate=1000.0, seed=99)), realtime=False)
-    # the clients' densities are drawn before the clock starts: they arrive with the requests
-    reqs = attach_payloads(request_stream(a.serve_requests, rate=200.0))
-    clocks = ClockSampler(torch.cuda.current_device())
-    clocks.start()
+    reqs = attach_payloads(request_stream(n_requests, rate=200.0))
+    if clocks is not None:
+        clocks.start()
     l0 = lib.gbsimp_launch_count()
-    srv = FEMServer(max_slots=24)
+    srv = FEMServer(max_slots=24, round_iters=SERVE_ROUND_ITERS)
     summ = srv.run(reqs, realtime=True)
     launches = lib.gbsimp_launch_count() - l0
-    clk = clocks.stop()
-    plain_reqs = request_stream(a.serve_requests, rate=200.0)[: max(50, a.serve_requests // 10)]
+    clk = clocks.stop() if clocks is not None else None
+    plain_reqs = request_stream(n_requests, rate=200.0)[:n_plain]
     for p_req, req in zip(plain_reqs, reqs):  # the same requests with the same payloads
         p_req.density = req.density
-    plain = FEMServer(max_slots=1).run(plain_reqs, realtime=False)
+    plain = FEMServer(max_slots=1, round_iters=0).run(plain_reqs, realtime=False)
+    # the served rate over the same first requests, for a like-for-like ratio
+    first = sorted(reqs, key=lambda r: r.arrival)[:n_plain]
+    plain_rate = plain["solves_per_s"]
+    return {"workload": f"{n_requests} requests, Poisson arrivals at 200/s, edges U{{24,32,48,64,96}} (cubic), "
+                        "loads U{cantilever tip, top patch, torsion}, ~10% repeats, GRF densities as payload, "
+                        "FP32 PCG + FP64 correction to rtol 1e-8",
+            "unit": "FEM solves/s", "served": summ, "served_solves_per_s": summ["solves_per_s"],
+            "plain_solves_per_s": plain_rate, "served_over_plain": summ["solves_per_s"] / plain_rate,
+            "plain": {"requests": plain["requests"], "note": "first requests of the same stream, one slot, "
+                                                             "all queued at t=0"},
+            "served_first_mean_ms": float(np.mean([r.latency for r in first]) * 1e3),
+            "round_iters": SERVE_ROUND_ITERS, "max_slots": 24, "gpu_launches": int(launches), "clocks": clk}
+
+
+def measure_c4(peak: float):
+    """192x96x96 (1,769,472 elements, 5,447,811 DOFs) on seeded densities U(0.1, 1) with the
+    line-load case's Dirichlet mask: the one-kernel PCG iteration (gbsimp_time_pcg_apply: 50
+    graph-replayed launches, CUDA events on the stream, frozen scalars) and the bare stiffness
+    apply y = D K(x) D p (apply_modal_kernel<PLAIN>), warm (20 back-to-back launches, median of
+    5) and cold (one launch after a 256 MB L2 flush, median of 5). The PCG vectors (about
+    218 MB) do not fit in the 129 MB L2."""
+    import torch
+
+    from genpipeline_gb300 import _lib as L
+    from genpipeline_gb300 import bcs
+    from genpipeline_gb300.engine import get_engine, n_dof, n_elem
+
+    eng = get_engine()
+    grid = (192, 96, 96)
+    law = L.make_law("modified", 3.0)
+    ne, nd = n_elem(grid), n_dof(grid)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.rand(ne, device="cuda", generator=gen) * 0.9 + 0.1
+    p = torch.randn(nd, device="cuda", generator=gen)
+    y = torch.empty_like(p)
+    _, fixed = bcs.edge_line_load(*grid)
+    mask = torch.as_tensor(bcs.node_mask(*grid, fixed), device="cuda")
+    flush = torch.empty(256 * 2**20, dtype=torch.uint8, device="cuda")
+    per_launch = eng.time_pcg_apply(grid, law, x, mask, reps=50)
+    pcg_bytes = 4 * (10 * nd + ne)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) * 1e-3
+
+    for _ in range(3):
+        eng.apply(grid, law, x, p, mask, y)
+    torch.cuda.synchronize()
+    warm = statistics.median(timed(lambda: [eng.apply(grid, law, x, p, mask, y) for _ in range(20)]) / 20
+                             for _ in range(5))
+    cold = []
+    for _ in range(5):
+        flush.zero_()
+        cold.append(timed(lambda: eng.apply(grid, law, x, p, mask, y)))
+    cold = statistics.median(cold)
+    apply_bytes = 4 * (2 * nd + ne)
+    return {"workload": "192x96x96, densities U(0.1,1) seed 0, x=0 clamped (line-load case's mask)",
+            "pcg_iteration": {"kernel": "apply_modal_kernel<CG>", "launch_us": per_launch * 1e6,
+                              "alg_bytes_per_launch": pcg_bytes, "achieved_GBs": pcg_bytes / per_launch / 1e9,
+                              "frac": pcg_bytes / per_launch / 1e9 / peak, "traffic": _profiled_traffic("c4")},
+            "bare_apply": {"kernel": "apply_modal_kernel<PLAIN>", "warm_us": warm * 1e6, "cold_us": cold * 1e6,
+                           "alg_bytes_per_launch": apply_bytes, "cold_GBs": apply_bytes / cold / 1e9,
+                           "cold_frac": apply_bytes / cold / 1e9 / peak, "warm_frac": apply_bytes / warm / 1e9 / peak},
+            "peak_GBs": peak}
+
+
+def run_serve(a):
+    """The serving stream alone (--workload serve), with its own JSON line."""
+    import torch
+
+    clocks = ClockSampler(torch.cuda.current_device())
+    res = measure_serving(a.serve_requests, max(50, a.serve_requests // 10), clocks)
+    summ, clk, launches = res["served"], res["clocks"], res["gpu_launches"]
+    plain = {"requests": res["plain"]["requests"], "solves_per_s": res["plain_solves_per_s"]}
     line = {"metric": METRIC, "value": summ["solves_per_s"], "unit": "FEM solves/s", "n_gpus": 1,
             "steps": summ["requests"], "warmup": 40, "ms_per_step": 1e3 / summ["solves_per_s"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (FP64 outer residual, dots, compliance)", "data": "synthetic", "impl": "ours",
             "config": {"workload": "fem_serving_stream", "requests": summ["requests"], "rate_per_s": 200.0,
                        "edges": [24, 32, 48, 64, 96], "loads": ["cantilever", "top_patch", "torsion"],
-                       "repeat_fraction": 0.1, "rtol": 1e-8, "max_slots": 24,
+                       "repeat_fraction": 0.1, "rtol": 1e-8, "max_slots": 24, "round_iters": SERVE_ROUND_ITERS,
                        "payload": "densities arrive with the requests (drawn by the client before the run); "
                                   "the server builds each (edge, load) case once"},
             "serving": summ, "plain_one_at_a_time": {"requests": plain["requests"], "solves_per_s": plain["solves_per_s"],
@@ -596,36 +691,44 @@ def run_ours(a):
         prob.solve()
         c_gpu = prob.compliance()
         prob.u.copy_(gpu_u0)
-        c0 = time.perf_counter()
-        for _ in range(a.cpu_sample_steps):
+        n_cpu = max(1, a.cpu_sample_steps)
+        per_step = []
+        for k in range(n_cpu):
+            c0 = time.perf_counter()
             ost.step()
-            if _ == 0:
+            per_step.append(time.perf_counter() - c0)
+            if k == 0:
                 c_cpu = ost.compliance
-        tc = time.perf_counter() - c0
+        tc = statistics.median(per_step)
         rel_err = abs(c_gpu - c_cpu) / abs(c_cpu)
-        cpu = {"value": a.cpu_sample_steps / tc, "unit": UNIT, "cores": _cpu_threads(), "kind": "port",
-               "sample": f"{a.cpu_sample_steps} OC iteration(s) of the same trajectory, started from the "
+        cpu = {"value": 1.0 / tc, "unit": UNIT, "cores": _cpu_threads(), "kind": "port",
+               "sample": f"median of {n_cpu} OC iterations of the same trajectory, started from the "
                          f"GPU state after {a.warmup + a.steps} iterations (FP64 C/OpenMP oracle)",
-               "seconds": tc}
+               "seconds_per_step": per_step}
 
     fem = None
     rows = None
+    c4 = None
+    serving = None
     if rank == 0 and a.workload == "simp64" and not a.no_batch:
         fem = measure_batch()
     if rank == 0 and a.workload == "simp64" and not a.no_rows:
         rows = measure_rows(prob.xphys)
+    if rank == 0 and a.workload == "simp64" and not a.no_c4:
+        c4 = measure_c4(_measured_peak()[0])
+    if rank == 0 and a.workload == "simp64" and a.line_serve_requests > 0:
+        serving = measure_serving(a.line_serve_requests, 50, ClockSampler(dev.index if dev.index is not None else 0))
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": tmax / a.steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 outer residual, dots, compliance)",
                 "data": "synthetic", "impl": "ours",
-                "config": dict(WORKLOAD, l2="L2 flushed (256 MB write) before every timed step; inside a step "
-                                         "the PCG vectors stay in L2 when they fit (64^3: ~36 MB)",
-                               parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+                "config": dict(WORKLOAD, **_line_keys(world)),
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clk, "pcg_iterations_per_step": pcg_iters / a.steps,
-                "compliance_rel_err_vs_fp64_oracle": rel_err, "fem_solves_per_s": fem, "next_rows": rows}
+                "compliance_rel_err_vs_fp64_oracle": rel_err, "fem_solves_per_s": fem, "c4": c4,
+                "serving": serving, "next_rows": rows}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -655,7 +758,7 @@ def run_reference(a):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": t / a.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": dict(WORKLOAD, solver="FP64 Jacobi-PCG to rtol 1e-8, warm start (oracle port)"),
+            "config": dict(WORKLOAD, **_line_keys(world), solver="FP64 Jacobi-PCG to rtol 1e-8, warm start (oracle port)"),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"OC iterations {a.warmup}..{a.warmup + a.steps - 1} of the trajectory "
                                        "(FP64 C/OpenMP restatement of SIMPSolver, all host threads)"},
