@@ -239,8 +239,9 @@ def simp_gpu_run(grid, rmin, penal, f, fixed, volfrac, n_iters, preserved=None, 
     - the early stop after three relative compliance changes below 1% (:113-125).
     ``_solve`` solves directly (SuperLU) whenever the grid has fewer than 50,000 DOFs
     (:581-588), whatever the tolerance: those solves run here to ``exact_tol``.
-    ``fp32_storage`` rounds dc, the filtered dc, x and xPhys to float32 where a
-    single-precision implementation stores them: the drift that storage alone causes.
+    ``fp32_storage`` (True, or "keep_start" to leave the initial design unrounded) rounds dc,
+    the filtered dc, x and xPhys to float32 where a single-precision implementation stores
+    them: the drift that storage alone causes.
     Returns dict(xphys, history, last_compliance, iterations)."""
     nx, ny, nz = grid
     ne = nx * ny * nz
@@ -276,7 +277,8 @@ def simp_gpu_run(grid, rmin, penal, f, fixed, volfrac, n_iters, preserved=None, 
     pmask = None if pres is None else pres.astype(np.uint8)
     r32 = (lambda a: a.astype(np.float32).astype(np.float64)) if fp32_storage else (lambda a: a)
     hs = r32(hs)
-    x, xphys = r32(x), r32(xphys)
+    if fp32_storage != "keep_start":  # "keep_start": the initial design stays exact
+        x, xphys = r32(x), r32(xphys)
     for i in range(n_iters):
         tol, max_iter = schedule(i)
         u = solve(u_prev, tol, max_iter)

