@@ -69,6 +69,8 @@ def _args():
     ap.add_argument("--line-serve-requests", type=int, default=300,
                     help="requests of the serving stream inside the default line (0: skip it)")
     ap.add_argument("--no-c4", action="store_true", help="skip the 192x96x96 kernel timings of the default line")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip timing the reference's own GPU FEM solve (from baseline/_ref) in the default line")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched FEM (served vs plain) measurement")
     ap.add_argument("--no-rows", action="store_true",
                     help="skip the evaluator / STL / generator measurements")
@@ -545,6 +547,98 @@ def measure_c4(peak: float):
             "peak_GBs": peak}
 
 
+# The reference's own GPU path, run unmodified from its installed copy (baseline/_ref) in a
+# child process: GPUVoxelFEM(voxels).solve() (gpu_fem_solver.py:76-133), i.e. COO -> CSR
+# assembly, boundary conditions and SIMPSolverGPU._solve (torch sparse PCG, tol 1e-3, 200
+# iterations) on the same voxel grid as ours.
+_REF_GPU_CHILD = r"""
+import json, sys, time
+import numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+from genpipeline.fem.gpu_fem_solver import GPUVoxelFEM
+vox = np.load(sys.argv[2])
+reps = int(sys.argv[3])
+if len(sys.argv) > 4:  # the SPD element injected in place of the literal table (one method)
+    from genpipeline.topology.simp_solver_gpu import SIMPSolverGPU
+    ke = np.load(sys.argv[4])
+    SIMPSolverGPU._get_Ke = staticmethod(lambda nu=0.3: ke)
+r = GPUVoxelFEM(vox, device="cuda").solve()
+torch.cuda.synchronize()
+ts = []
+for _ in range(reps):
+    fem = GPUVoxelFEM(vox, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = fem.solve()
+    torch.cuda.synchronize()
+    ts.append(time.perf_counter() - t0)
+print("REFGPU " + json.dumps({"seconds": ts, "result": {k: float(v) for k, v in r.items()}}))
+"""
+
+
+def measure_reference_gpu(n: int = 32, reps: int = 5, timeout: float = 240.0):
+    """Per-solve time of the reference's GPUVoxelFEM.solve and of this library's drop-in on one
+    n^3 voxel grid (GRF densities, seed 5; x_min clamped, 1000 N in -z spread over x_max; tol
+    1e-3 / 200 PCG iterations on both sides, as gpu_fem_solver.py:96 asks). The reference runs
+    twice: as shipped, and with the SPD element injected (SIMPSolverGPU._get_Ke only), since
+    as shipped it assembles its literal element table, which is not symmetric positive
+    definite. Unavailable when the reference copy is absent (it is installed into
+    baseline/_ref, not committed)."""
+    import tempfile
+
+    import numpy as np
+    import torch
+
+    from genpipeline_gb300 import designs as D
+    from genpipeline_gb300.engine import Engine
+    from genpipeline_gb300.fem import GPUVoxelFEM
+
+    ref_dir = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(ref_dir, "genpipeline")):
+        return {"unavailable": "the reference is not installed in baseline/_ref"}
+    vox = D.grf_density((n, n, n), 5).reshape(n, n, n).astype(np.float32)
+    runs = {}
+    with tempfile.TemporaryDirectory() as td:
+        path, kpath = os.path.join(td, "vox.npy"), os.path.join(td, "ke.npy")
+        np.save(path, vox)
+        np.save(kpath, Engine.ke_quadrature(0.3, 1.0))
+        for name, extra in (("as_shipped", []), ("spd_element", [kpath])):
+            try:
+                out = subprocess.run([sys.executable, "-c", _REF_GPU_CHILD, ref_dir, path, str(reps), *extra],
+                                     capture_output=True, text=True, timeout=timeout)
+            except subprocess.TimeoutExpired:
+                return {"unavailable": f"the reference's solve did not finish within {timeout:.0f} s"}
+            line = [ln for ln in out.stdout.splitlines() if ln.startswith("REFGPU ")]
+            if out.returncode != 0 or not line:
+                return {"unavailable": f"reference run failed (rc {out.returncode}): {out.stderr.strip()[-300:]}"}
+            runs[name] = json.loads(line[-1][7:])
+    GPUVoxelFEM(vox).solve()
+    torch.cuda.synchronize()
+    ours_t = []
+    for _ in range(reps):
+        fem = GPUVoxelFEM(vox)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fem.solve()
+        torch.cuda.synchronize()
+        ours_t.append(time.perf_counter() - t0)
+    ref = runs["as_shipped"]
+    tr, to = statistics.median(ref["seconds"]), statistics.median(ours_t)
+    return {"workload": f"GPUVoxelFEM.solve, {n}^3 GRF voxels (seed 5), {3 * (n + 1) ** 3} DOFs, x_min clamped, "
+                        "1000 N -z over x_max, tol 1e-3 / 200 iterations",
+            "reference": "genpipeline GPUVoxelFEM (torch sparse COO->CSR assembly + SIMPSolverGPU._solve), "
+                         "unmodified, in a child process",
+            "reference_s_per_solve": tr, "ours_s_per_solve": to, "speedup": tr / to,
+            "reference_result": ref["result"], "ours_result": {k: float(v) for k, v in r.items()},
+            "reference_spd_element": {"s_per_solve": statistics.median(runs["spd_element"]["seconds"]),
+                                      "result": runs["spd_element"]["result"]},
+            "note": "as shipped, the reference assembles its literal element table, which is not symmetric "
+                    "positive definite, so its CG result is not a solution of an elasticity problem; with the "
+                    "SPD element injected both sides solve the same system to 1e-3 (FP64 oracle compliance "
+                    "680056.7 at rtol 1e-10)",
+            "reps": reps}
+
+
 def run_serve(a):
     """The serving stream alone (--workload serve), with its own JSON line."""
     import torch
@@ -718,6 +812,9 @@ def run_ours(a):
         c4 = measure_c4(_measured_peak()[0])
     if rank == 0 and a.workload == "simp64" and a.line_serve_requests > 0:
         serving = measure_serving(a.line_serve_requests, 50, ClockSampler(dev.index if dev.index is not None else 0))
+    ref_gpu = None
+    if rank == 0 and a.workload == "simp64" and not a.no_reference_gpu:
+        ref_gpu = measure_reference_gpu()
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
@@ -728,7 +825,7 @@ def run_ours(a):
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clk, "pcg_iterations_per_step": pcg_iters / a.steps,
                 "compliance_rel_err_vs_fp64_oracle": rel_err, "fem_solves_per_s": fem, "c4": c4,
-                "serving": serving, "next_rows": rows}
+                "serving": serving, "reference_gpu_path": ref_gpu, "next_rows": rows}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
