@@ -234,7 +234,8 @@ __device__ __forceinline__ float ld_vec(const float *p) {
 }
 
 // One sliding-window pass of a CTA over its (flat tile, x segment): y = D K D p on the owned
-// nodes (PLAIN), or one PCG iteration with y = w_{i+1} (CG modes). sums[] receives this
+// nodes (PLAIN; x = densities), or one PCG iteration with y = w_{i+1} (CG modes; x = the
+// element moduli E(x_e), computed once per solve). sums[] receives this
 // thread's FP32 shares of r.u, w.u and r.r (CG modes). Every node vector must be 16-byte
 // aligned. pre(alpha, beta, alpha_prev) runs once the first plane's copies are in flight (the
 // step's scalars can be formed meanwhile); when it returns false the pass stops there
@@ -346,11 +347,11 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
         }
         bphase ^= 1u;
     };
+    const int64_t full = NW & ~(int64_t)3;  // words of the vectors in whole 16-byte groups
     auto issue_plane = [&](int j) {
-        const PlaneW P = plane_w(j);
         {
-            const int64_t full = NW & ~(int64_t)3;  // words in whole groups
             if (tid == 0) {
+                const PlaneW P = plane_w(j);
                 unsigned nfull = 0, nown = 0;
                 int64_t g0 = 0, o0 = 0;
                 if (P.pv) {
@@ -376,8 +377,10 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                         if (a == 4 || cp.xmode)
                             bulk_copy_g2s(Raw + a * RW + (o0 - P.A), src_of(a) + o0, 4u * nown, &s_bar);
             }
-            if (P.pv && full < NW && full >= P.A) {  // the group cut by the end of the vectors
-                const int64_t ft = (full - P.A) >> 2;
+            // the group cut by the end of the vectors: only the last node plane reaches it
+            if (j == nx && full < NW) {
+                const PlaneW P = plane_w(j);
+                const int64_t ft = full >= P.A ? (full - P.A) >> 2 : (int64_t)P.nv;
                 if (ft < P.nv && (int)(ft % NT) == tid) {
                     const int f = (int)ft, cw0 = 4 * f - P.pad;
                     const int nb = 4 * (int)(NW - full);
@@ -530,9 +533,14 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
             ex[q] = eok[q] ? x[j * eplane + eoff[q]] : 0.0f;
         }
     };
+    // PLAIN: x holds densities and the law gives the moduli; CG modes: x already holds the
+    // moduli E(x_e) of the solve (issue_eplane leaves 0 outside the grid)
     auto commit_eplane = [&](int slot) {
-        Es2[slot * NT + tid] =
-            make_float2(eok[0] ? modulus(law, ex[0]) : 0.0f, eok[1] ? modulus(law, ex[1]) : 0.0f);
+        if (CG)
+            Es2[slot * NT + tid] = make_float2(ex[0], ex[1]);
+        else
+            Es2[slot * NT + tid] =
+                make_float2(eok[0] ? modulus(law, ex[0]) : 0.0f, eok[1] ? modulus(law, ex[1]) : 0.0f);
     };
     // Index in Bdf of the z+1-side contribution (cy, c = 0) of element e - 1, for an element e
     // in lane 0; component c adds 2 c.
@@ -545,12 +553,19 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
     // bl[q] for lane 0 (element l - 1 in lane 31 of the previous warp), bm[q] for the node
     // whose y-neighbour element m = l - NZ sits in lane 0; -1 where there is none.
     int bl[EPT], bm[EPT];
+    // node l of this thread: owned-range test (node_ok), slot of its y-neighbour element m in
+    // the y-slots (zi), and its flat index in the plane (loop-invariant)
+    int zi[EPT], nflat[EPT];
+    bool node_ok[EPT];
 #pragma unroll
     for (int q = 0; q < EPT; ++q) {
         const int l = tid + q * NT, mm = l - NZ;
         const bool node = l >= H;  // then l >= 1 and m >= 1
         bl[q] = node && lane == 0 ? bd_index(l, 0) : -1;
         bm[q] = node && (mm & 31) == 0 ? bd_index(mm, 1) : -1;
+        nflat[q] = F0 - H + l;
+        node_ok[q] = node && nflat[q] < S;
+        zi[q] = mm >= NT ? 2 * (mm - NT) + 1 : 2 * mm;
     }
 
     // ---- prologue: node planes x0, x0 + 1 and element plane x0 (the raw buffers hold one
@@ -660,26 +675,30 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
 #pragma unroll
         for (int q = 0; q < EPT; ++q) {
             const int l = tid + q * NT;
-            const int flat = F0 - H + l;
-            if (l >= H && out_plane && flat < S) {
-                const int m = l - NZ;  // element whose y+1 corners touch node l (m >= 1)
-                const int mi = m >= NT ? 2 * (m - NT) + 1 : 2 * m;
-                const float uc[3] = {Pu[3 * l], Pu[3 * l + 1], Pu[3 * l + 2]};
-                float *yo = y + 3 * ((int64_t)i * S + flat);
+            if (node_ok[q] && out_plane) {
+                // zi[q]: the y+1 corners of element l - NZ (>= 1), which touch node l
+                float yc[3];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    float s = (q ? z0[c].y : z0[c].x) + Z1f[c * 2 * NT + mi];
+                    float s = (q ? z0[c].y : z0[c].x) + Z1f[c * 2 * NT + zi[q]];
                     const float tl = Bdf[max(bl[q], 0) + 2 * c], tm = Bdf[max(bm[q], 0) + 2 * c];
                     s += bl[q] >= 0 ? tl : 0.0f;
                     s += bm[q] >= 0 ? tm : 0.0f;
                     // PCG modes leave w unmasked: 1/diag = 0 keeps u, p and x at zero on fixed
                     // DOFs whatever w holds there, and r.r skips them (the plain apply masks)
-                    const float yc = (!CG && ((om[q] >> c) & 1)) ? 0.0f : s;
-                    if (CG) g_wu = fmaf(uc[c], yc, g_wu);
-                    if (shared)
-                        atomicAdd(yo + c, yc);
-                    else
-                        yo[c] = yc;
+                    yc[c] = (!CG && ((om[q] >> c) & 1)) ? 0.0f : s;
+                }
+                if (CG) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) g_wu = fmaf(Pu[3 * l + c], yc[c], g_wu);
+                }
+                float *yo = y + 3 * ((int64_t)i * S + nflat[q]);
+                if (shared) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) atomicAdd(yo + c, yc[c]);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) yo[c] = yc[c];
                 }
             }
         }

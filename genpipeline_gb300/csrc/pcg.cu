@@ -49,6 +49,7 @@ struct PcgWs {
     float *r, *dinv, *p0, *p1, *ap, *r1, *s0, *s1, *w2;
     double *partials;
     size_t partial_count;
+    float *E;  // element moduli E(x_e) of the solve (single-reduction form: read by every launch)
 };
 
 static inline bool use_modal(const gbsimp_ctx *ctx, int nz) { return ctx->modal_ok && modal_fits(nz); }
@@ -80,7 +81,7 @@ static int check_modal_partials(const gbsimp_ctx *ctx, int nx, int ny, int nz, c
 static size_t pcg_ws_bytes_impl(int nx, int ny, int nz) {
     const size_t nd = (size_t)n_dof_of(nx, ny, nz);
     return 256 + al256(sizeof(PcgScalars)) + 9 * al256(nd * sizeof(float)) +
-           al256(pcg_partials(nx, ny, nz) * sizeof(double));
+           al256(pcg_partials(nx, ny, nz) * sizeof(double)) + al256((size_t)nx * ny * nz * sizeof(float));
 }
 
 // Sub-buffers start on 256-byte boundaries whatever the alignment of `ws` (the size has
@@ -100,7 +101,16 @@ static PcgWs pcg_ws(void *ws, int nx, int ny, int nz) {
     }
     w.partials = (double *)p;
     w.partial_count = pcg_partials(nx, ny, nz);
+    p += al256(w.partial_count * sizeof(double));
+    w.E = (float *)p;
     return w;
+}
+
+// E[e] = E(x_e): the single-reduction kernels read the moduli instead of evaluating the law
+// per element and launch (the same FP32 function of the same inputs, so the same values).
+__global__ void moduli_f32_kernel(int64_t n, Law<float> law, const float *__restrict__ x, float *E) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        E[e] = modulus(law, x[e]);
 }
 
 static CgArgs cg_args(const PcgWs &w, float *u) {
@@ -393,8 +403,8 @@ static int read_scalars(const PcgScalars *d, PcgScalars *h, cudaStream_t st) {
 static int pcg_iteration(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
                          const uint8_t *mask, float *u, const PcgWs &w, cudaStream_t st, cudaEvent_t after_k1,
                          int phase) {
-    if (use_modal(ctx, nz)) {
-        int rc = launch_modal<MODE_CG>(ctx, nx, ny, nz, law, x, nullptr, nullptr, mask, cg_args(w, u), st, phase);
+    if (use_modal(ctx, nz)) {  // reads the moduli w.E of the setup, not x
+        int rc = launch_modal<MODE_CG>(ctx, nx, ny, nz, law, w.E, nullptr, nullptr, mask, cg_args(w, u), st, phase);
         if (rc) return rc;
         if (after_k1) GBS_CUDA_TRY(cudaEventRecord(after_k1, st));
         return GBS_OK;
@@ -667,7 +677,7 @@ static int fused_plan(const gbsimp_ctx *ctx, const FusedItem *items, int n, Fuse
         D.tiles = tiles[i];
         D.block0 = block0;
         D.nblk = tiles[i] * nseg[i];
-        D.x = itm.x;
+        D.x = itm.w.E;  // the moduli of the design's setup
         D.mask = itm.mask;
         D.ca = cg_args(itm.w, itm.u);
         block0 += D.nblk;
@@ -899,6 +909,11 @@ static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp
     if (!(flags & SETUP_KEEP_DINV)) {
         dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, law, ctx->kef, x, mask, w.dinv);
         GBS_LAUNCH_CHECK("dinv_kernel");
+        if (use_modal(ctx, nz)) {
+            const int64_t ne = (int64_t)nx * ny * nz;
+            moduli_f32_kernel<<<vec_blocks(ctx, ne), 256, 0, st>>>(ne, law, x, w.E);
+            GBS_LAUNCH_CHECK("moduli_f32_kernel");
+        }
     }
     const int max_trips = (max_iter + kLoopUnroll - 1) / kLoopUnroll + 2;
     // q = D K D u into `qbuf`, or zeros when u is known to be zero
@@ -1413,6 +1428,8 @@ extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, co
     fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.p1);
     fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, xu);
     if (modal) {  // launches alternate the buffer parity: give both parities the same state
+        const int64_t ne = (int64_t)nx * ny * nz;
+        moduli_f32_kernel<<<vec_blocks(ctx, ne), 256, 0, st>>>(ne, law, x, w.E);
         fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 1.0f, w.r1);
         fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.ap);
         fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.s0);
@@ -1435,7 +1452,7 @@ extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, co
     PcgArgs pa{w.r, w.dinv, w.p0, w.p1, xu, w.partials, w.sc};
     for (int i = 0; i < reps && rc == GBS_OK; ++i) {
         if (modal) {
-            rc = launch_modal<MODE_CG>(ctx, nx, ny, nz, law, x, nullptr, nullptr, node_mask, cg_args(w, xu), gc->cap,
+            rc = launch_modal<MODE_CG>(ctx, nx, ny, nz, law, w.E, nullptr, nullptr, node_mask, cg_args(w, xu), gc->cap,
                                        i % 6);
         } else {
             TileArgs<float> A{nx, ny, nz, x, nullptr, w.ap, node_mask};
