@@ -236,20 +236,24 @@ def batch_designs():
 
 def measure_batch(repeats=2):
     """FEM solves/s of the 8-design batch: plain = one solve per design (graph-loop PCG, one
-    design on the GPU at a time); served = the designs together in gbsimp_batch_round
-    (persistent kernel, each design on its share of the SMs). Cold starts (u0 = 0) both."""
+    design on the GPU at a time); served = the designs together in gbsimp_batch_round with the
+    configuration the autotuner chose for this grid class (timed once per candidate during the
+    warm-up, then cached); served_rule = the untuned default (one persistent launch, SMs in
+    proportion to element counts). Cold starts (u0 = 0) everywhere."""
     import torch
 
+    from genpipeline_gb300 import autotune as A
     from genpipeline_gb300.batch import BatchFEM, solve_plain
 
     solve_plain(batch_designs())  # warm-up: graphs, code paths
-    BatchFEM().solve_all(batch_designs())
+    tuner = A.default_tuner()
+    BatchFEM(tuner=tuner).solve_all(batch_designs())  # tunes this grid class (cached afterwards)
     res = {}
-    for name in ("plain", "served"):
+    for name in ("plain", "served", "served_rule"):
         best = None
         for _ in range(repeats):
             ds = batch_designs()
-            bf = BatchFEM()
+            bf = BatchFEM(tuner=tuner) if name == "served" else BatchFEM()
             for d in ds:
                 bf.upload(d)
             torch.cuda.synchronize()
@@ -267,6 +271,8 @@ def measure_batch(repeats=2):
                         "FP32 PCG + FP64 correction to rtol 1e-8, cold start",
             "plain": 8 / res["plain"][0], "served": 8 / res["served"][0],
             "served_over_plain": res["plain"][0] / res["served"][0],
+            "served_rule": 8 / res["served_rule"][0],
+            "autotune": A.summary(tuner, [d.grid for d in batch_designs()]),
             "max_compliance_rel_diff": diff,
             "pcg_iterations": sum(d.stats["iterations"] for d in res["served"][2]),
             "unit": "FEM solves/s"}

@@ -50,17 +50,58 @@ class FEMDesign:
 class BatchFEM:
     """Runs gbsimp_batch_round over a changing set of designs. ``round_iters`` > 0 bounds the
     inner PCG iterations of one round (a solve still running is paused and resumes in the
-    next round), so that a serving loop regains control every few milliseconds."""
+    next round), so that a serving loop regains control every few milliseconds. With
+    ``autotune`` (or a ``tuner``), ``solve_all`` first picks the form, SM shares and designs per
+    launch for the batch's grid class (autotune.BatchTuner: every candidate timed once on copies
+    of the designs, the choice cached per grid class)."""
 
     def __init__(self, engine: Optional[Engine] = None, law: Optional[L.Law] = None, rtol: float = 1e-8,
                  inner_rtol: float = 1e-4, max_iter: int = 200000, max_outer: int = 30, fused: bool = True,
-                 round_iters: int = 0):
+                 round_iters: int = 0, autotune: bool = False, tuner=None):
         self.eng = engine or get_engine()
         self.law = law or L.make_law("modified", 3.0)
+        self._args = dict(rtol=rtol, inner_rtol=inner_rtol, max_iter=max_iter, max_outer=max_outer)
         self.opts = Engine.opts(rtol=rtol, inner_rtol=inner_rtol, max_iter=max_iter, max_outer=max_outer,
                                 fused=int(fused), check_every=int(round_iters))
         self.items: List[FEMDesign] = []
         self._structs = None
+        if tuner is None and autotune:
+            from .autotune import default_tuner
+
+            tuner = default_tuner()
+        self.tuner = tuner
+        self.config = None  # the autotune.BatchConfig applied by the last solve_all (None: the options as given)
+
+    def apply_config(self, cfg) -> None:
+        """Sets the batch parameters of an autotune.BatchConfig."""
+        self.opts.fused = int(cfg.fused)
+        self.opts.batch_share = int(cfg.batch_share)
+        self.opts.batch_group = int(cfg.batch_group)
+        self.config = cfg
+
+    def _trial(self, designs: List[FEMDesign], cfg) -> float:
+        """Seconds of one whole solve of copies of `designs` under cfg: the same device densities,
+        loads and masks, their warm starts copied, new displacements and workspaces (the designs
+        themselves are left as they are)."""
+        from .autotune import timed
+
+        bf = BatchFEM(self.eng, self.law, round_iters=int(self.opts.check_every), **self._args)
+        bf.apply_config(cfg)
+        copies = []
+        for d in designs:
+            if d.dx is None:
+                self.upload(d)
+            c = FEMDesign(d.grid, d.x, d.f, d.fixed_dofs, tag=None)
+            c.dx, c.df, c.dmask = d.dx, d.df, d.dmask
+            c.du = (d.u0.to(device=self.eng.device, dtype=torch.float64).clone() if d.u0 is not None
+                    else torch.zeros(n_dof(d.grid), dtype=torch.float64, device=self.eng.device))
+            c.ws = torch.empty_like(d.ws)
+            copies.append(c)
+        out = []
+        t = timed(lambda: out.extend(bf._solve_loop(copies)), torch.cuda.synchronize)
+        if len(out) != len(copies) or any(c.stats["status"] != L.GBS_OK for c in out):
+            raise RuntimeError(f"trial of {cfg} did not solve every design")
+        return t
 
     def upload(self, d: FEMDesign) -> FEMDesign:
         dev = self.eng.device
@@ -117,6 +158,14 @@ class BatchFEM:
         return False
 
     def solve_all(self, designs: List[FEMDesign]) -> List[FEMDesign]:
+        if self.tuner is not None and designs:
+            for d in designs:
+                if d.dx is None:
+                    self.upload(d)
+            self.apply_config(self.tuner.tune([d.grid for d in designs], lambda cfg: self._trial(designs, cfg)))
+        return self._solve_loop(designs)
+
+    def _solve_loop(self, designs: List[FEMDesign]) -> List[FEMDesign]:
         for d in designs:
             self.add(d)
         out = []

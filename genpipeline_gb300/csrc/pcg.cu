@@ -606,10 +606,14 @@ struct FusedPlan {
 };
 
 // Plans the launch of up to kMaxFused initialised designs: the CTAs of the GPU are shared in
-// proportion to the designs' element counts (at least one segment of flat tiles each).
-// Returns GBS_EINVAL when the designs cannot all be resident at once (the caller then
-// iterates them with the graph loop, or splits them over several launches). Host only.
-static int fused_plan(const gbsimp_ctx *ctx, const FusedItem *items, int n, FusedPlan *plan) {
+// proportion to the designs' element counts (share 0) or element counts x longest extent
+// (share 1: Jacobi-PCG iteration counts grow about with the longest extent, so the designs
+// finish together instead of small ones leaving their SMs idle while a large one runs), at
+// least one segment of flat tiles each. Returns GBS_EINVAL when the designs cannot all be
+// resident at once (the caller then iterates them with the graph loop, or splits them over
+// several launches). Host only. A paused design may be resumed under another plan: its state
+// is the iteration's scalars and vectors, which do not depend on the segmentation.
+static int fused_plan(const gbsimp_ctx *ctx, const FusedItem *items, int n, FusedPlan *plan, int share = 0) {
     if (n <= 0 || n > kMaxFused || !ctx->modal_ok) return GBS_EINVAL;
     bool small = true;
     int max_nz = 0;
@@ -637,20 +641,21 @@ static int fused_plan(const gbsimp_ctx *ctx, const FusedItem *items, int n, Fuse
     const int per_sm = modal_resident(ctx, kern, reg_cache[small ? 0 : 1][dev], smem);
     const int total = per_sm * (ctx->num_sms > 0 ? ctx->num_sms : 148);
     int tiles[kMaxFused], nseg[kMaxFused], seglen[kMaxFused];
-    double welem = 0.0;
+    double weight[kMaxFused], wsum = 0.0;
     int need = 0;
     for (int i = 0; i < n; ++i) {
         const int F = kModalNT * kModalEPT - (items[i].nz + 2);
         const int S = (items[i].ny + 1) * (items[i].nz + 1);
         tiles[i] = (S + F - 1) / F;
         need += tiles[i];
-        welem += (double)items[i].nx * items[i].ny * items[i].nz;
+        const int ext = std::max(items[i].nx, std::max(items[i].ny, items[i].nz));
+        weight[i] = (double)items[i].nx * items[i].ny * items[i].nz * (share == 1 ? (double)ext : 1.0);
+        wsum += weight[i];
     }
     if (need > total) return GBS_EINVAL;
     int used = 0;
     for (int i = 0; i < n; ++i) {
-        const double share = (double)items[i].nx * items[i].ny * items[i].nz / welem;
-        int s = (int)((double)total * share / tiles[i]);
+        int s = (int)((double)total * (weight[i] / wsum) / tiles[i]);
         s = s < 1 ? 1 : s;
         if (s > items[i].nx + 1) s = items[i].nx + 1;
         nseg[i] = s;
@@ -695,9 +700,9 @@ static int fused_plan(const gbsimp_ctx *ctx, const FusedItem *items, int n, Fuse
 // initialised designs in one cooperative launch (plan: fused_plan). A design that reaches the
 // budget keeps `done` clear and resumes in the next launch; its barrier counter restarts here.
 static int pcg_fused_batch(const gbsimp_ctx *ctx, const FusedItem *items, int n, const Law<float> &law,
-                           cudaStream_t st, int budget = 0) {
+                           cudaStream_t st, int budget = 0, int share = 0) {
     FusedPlan P;
-    int rc = fused_plan(ctx, items, n, &P);
+    int rc = fused_plan(ctx, items, n, &P, share);
     if (rc) return rc;
     for (int i = 0; i < n; ++i)
         GBS_CUDA_TRY(cudaMemsetAsync(&items[i].w.sc->bar_count, 0, sizeof(unsigned), st));
@@ -1696,12 +1701,14 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
         SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
         return FusedItem{it.nx, it.ny, it.nz, it.x, it.node_mask, w.d32, pcg_ws(w.pcg, it.nx, it.ny, it.nz)};
     };
+    const int group = o->batch_group > 0 && o->batch_group < kMaxFused ? o->batch_group : kMaxFused;
+    const int share = o->batch_share == 1 ? 1 : 0;
     auto fits = [&](const std::vector<int> &c) {
-        if (c.empty() || c.size() > (size_t)kMaxFused) return false;
+        if (c.empty() || c.size() > (size_t)group) return false;
         FusedItem fi[kMaxFused];
         for (size_t j = 0; j < c.size(); ++j) fi[j] = fitem(c[j]);
         FusedPlan P;
-        return fused_plan(ctx, fi, (int)c.size(), &P) == GBS_OK;
+        return fused_plan(ctx, fi, (int)c.size(), &P, share) == GBS_OK;
     };
     std::vector<int> order, graph_items;
     for (int i : act)
@@ -1734,7 +1741,7 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
     for (const auto &c : chunks) {
         FusedItem fi[kMaxFused];
         for (size_t j = 0; j < c.size(); ++j) fi[j] = fitem(c[j]);
-        if (pcg_fused_batch(ctx, fi, (int)c.size(), law, st, budget) == GBS_OK) {
+        if (pcg_fused_batch(ctx, fi, (int)c.size(), law, st, budget, share) == GBS_OK) {
             fused_items.insert(fused_items.end(), c.begin(), c.end());
             continue;
         }

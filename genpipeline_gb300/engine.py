@@ -209,9 +209,9 @@ class Engine:
 
     @staticmethod
     def opts(rtol=1e-8, inner_rtol=1e-4, max_iter=20000, max_outer=20, check_every=0, fused=0,
-             profile=0) -> L.SolveOpts:
+             profile=0, batch_share=0, batch_group=0) -> L.SolveOpts:
         return L.SolveOpts(float(rtol), float(inner_rtol), int(max_iter), int(max_outer), int(check_every),
-                           int(fused), int(profile), 0)
+                           int(fused), int(profile), int(batch_share), int(batch_group), 0)
 
     def pcg(self, grid: Grid, law: L.Law, x: torch.Tensor, b: torch.Tensor, mask: Optional[torch.Tensor],
             u: torch.Tensor, rtol=1e-6, max_iter=2000, check_every=0, key: str = "pcg", profile=False,

@@ -31,7 +31,9 @@
 extern "C" {
 #endif
 
-#define GBSIMP_ABI_VERSION 1
+/* 2: gbsimp_solve_opts gained batch_share and batch_group; gbsimp_solve_stats names its two
+ * library-owned fields (batched rounds with an iteration budget). */
+#define GBSIMP_ABI_VERSION 2
 
 enum {
     GBS_OK = 0,
@@ -78,6 +80,12 @@ typedef struct gbsimp_solve_opts {
                              its tolerance within the round */
     int32_t fused;        /* 1 = persistent fused PCG kernel, 0 = graph loop, one launch per iteration */
     int32_t profile;      /* 1 = time every PCG apply launch with CUDA events (stats) */
+    int32_t batch_share;  /* batched persistent launches: how the SMs are shared among the designs
+                             of one launch. 0 = in proportion to element counts; 1 = in proportion
+                             to element counts x longest grid extent (Jacobi-PCG iteration counts
+                             grow about with it, so the designs of a launch finish together) */
+    int32_t batch_group;  /* batched persistent launches: at most this many designs per launch
+                             (0 or more than 24: 24) */
     int32_t reserved;
 } gbsimp_solve_opts;
 

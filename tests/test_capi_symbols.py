@@ -34,7 +34,7 @@ def test_every_declared_symbol_is_exported_and_bound():
 
 def test_abi_version_and_errors():
     lib = L.load()
-    assert lib.gbsimp_abi_version() == 1
+    assert lib.gbsimp_abi_version() == 2
     with pytest.raises(L.GbsimpError) as ei:
         L.check(lib.gbsimp_ke_quadrature(0.6, 1.0, None))
     assert ei.value.code == L.GBS_EINVAL
@@ -72,14 +72,15 @@ def test_pcg_workspace_holds_the_one_kernel_partials():
     def al(b):
         return (b + 255) // 256 * 256
 
-    sc = lib.gbsimp_pcg_ws_bytes(1, 1, 1) - 256 - 9 * al(4 * 24) - al(8 * 12288)  # the scalars block
+    # the scalars block: total - slack - 9 vectors - partials - the element moduli (1 element)
+    sc = lib.gbsimp_pcg_ws_bytes(1, 1, 1) - 256 - 9 * al(4 * 24) - al(8 * 12288) - al(4)
     assert sc > 0 and sc % 256 == 0
     rng = np.random.default_rng(0)
     shapes = [(64, 64, 64), (192, 96, 96), (1, 300, 446), (2, 2000, 446), (1, 600, 400), (3, 1, 446), (1, 1, 1)]
     shapes += [(int(rng.integers(1, 64)), int(rng.integers(1, 2500)), int(rng.integers(1, 447))) for _ in range(300)]
     for nx, ny, nz in shapes:
         nd = 3 * (nx + 1) * (ny + 1) * (nz + 1)
-        part = lib.gbsimp_pcg_ws_bytes(nx, ny, nz) - 256 - sc - 9 * al(4 * nd)
+        part = lib.gbsimp_pcg_ws_bytes(nx, ny, nz) - 256 - sc - 9 * al(4 * nd) - al(4 * nx * ny * nz)
         f = 512 - (nz + 2)
         tiles = -(-(ny + 1) * (nz + 1) // f)
         for wave in (1, 152, 304, 608, 2048):

@@ -30,14 +30,18 @@ def _designs():
     return out
 
 
-@pytest.mark.parametrize("fused,round_iters", [(True, 0), (False, 0), (True, 7), (False, 30)])
-def test_batch_equals_single_solves(fused, round_iters):
+@pytest.mark.parametrize("fused,round_iters,share,group", [(True, 0, 0, 0), (False, 0, 0, 0), (True, 7, 0, 0),
+                                                           (False, 30, 0, 0), (True, 0, 1, 0), (True, 13, 1, 2)])
+def test_batch_equals_single_solves(fused, round_iters, share, group):
     """Whole inner solves per round, and rounds of 7 (persistent kernel) or 30 (graph loop, two
     12-iteration trips, then three) inner iterations after which each solve is paused and
-    resumed in the next round."""
+    resumed in the next round; SM shares by element count or by element count x extent, and
+    launches of at most two designs (a paused design then resumes under another plan)."""
     eng = Engine()
     single = solve_plain(_designs(), eng)
-    batch = BatchFEM(eng, fused=fused, round_iters=round_iters).solve_all(_designs())
+    bf = BatchFEM(eng, fused=fused, round_iters=round_iters)
+    bf.opts.batch_share, bf.opts.batch_group = share, group
+    batch = bf.solve_all(_designs())
     assert len(batch) == len(single)
     by_grid = {d.grid: d for d in batch}
     for s in single:
@@ -46,6 +50,27 @@ def test_batch_equals_single_solves(fused, round_iters):
         us, ub = s.du.cpu().numpy(), b.du.cpu().numpy()
         np.testing.assert_allclose(ub, us, rtol=0, atol=U_TOL * np.abs(us).max())
         assert b.compliance == pytest.approx(s.compliance, rel=C_TOL)
+
+
+def test_autotuned_batch_equals_single_solves(tmp_path):
+    """The tuner times every candidate on copies of the designs, applies the fastest, and the
+    solutions are those of single solves."""
+    from genpipeline_gb300.autotune import CANDIDATES, BatchTuner, summary
+
+    eng = Engine()
+    tuner = BatchTuner(cache_path=str(tmp_path / "tune.json"))
+    single = solve_plain(_designs(), eng)
+    bf = BatchFEM(eng, tuner=tuner)
+    batch = bf.solve_all(_designs())
+    grids = [d.grid for d in batch]
+    s = summary(tuner, grids)
+    assert bf.config is not None and tuner.choice(grids) == bf.config
+    assert len(s["trial_seconds"]) == len(CANDIDATES) and all(t > 0 for t in s["trial_seconds"].values())
+    by_grid = {d.grid: d for d in batch}
+    for d in single:
+        b = by_grid[d.grid]
+        assert b.stats["status"] == L.GBS_OK and b.stats["relres"] <= 1e-8, b.stats
+        assert b.compliance == pytest.approx(d.compliance, rel=C_TOL)
 
 
 def test_serving_results_equal_alone_and_in_the_mix():
