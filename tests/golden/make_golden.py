@@ -1,7 +1,7 @@
 """Generate the golden fixtures for the SIMP hot path by running the reference itself.
 
 This script imports the reference package ``genpipeline`` (a checkout given by
-``--reference``, default ``/root/reference``) and records what its own CPU code returns
+``--reference`` or the ``GENPIPELINE_REFERENCE`` environment variable) and records what its own CPU code returns
 on small seeded inputs. The GPU tests and the oracle tests compare against these
 ``.npz`` files; nothing at test time imports the reference.
 
@@ -328,7 +328,9 @@ def make_voxel(path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("GENPIPELINE_REFERENCE"),
+                    required=os.environ.get("GENPIPELINE_REFERENCE") is None,
+                    help="checkout of the reference repository (the directory holding genpipeline/)")
     ap.add_argument("--c0", action="store_true", help="also run the 50-iteration 32x16x16 case")
     ap.add_argument("--only-c0", action="store_true")
     ap.add_argument("--only-voxel", action="store_true", help="only the evaluator input step fixtures")

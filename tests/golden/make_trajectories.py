@@ -24,7 +24,7 @@ its solves stopped at rtol 1e-8, warm-started. Its distance from the FP64 trajec
 drift that FP32 storage alone causes, whatever the kernels: the GPU tests set their
 tolerances from it.
 
-Usage: ``python tests/golden/make_trajectories.py [--only c0|c1] [--threads N]``.
+Usage: ``python tests/golden/make_trajectories.py [--only c0|c0ref|c1] [--threads N]``.
 """
 from __future__ import annotations
 
