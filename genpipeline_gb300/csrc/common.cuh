@@ -221,6 +221,58 @@ __device__ __forceinline__ void block_sum_df(df32 (&v)[K], float2 *scratch) {
     }
 }
 
+// Unnormalised double-float values for the element products of the outer residual and of the
+// sensitivities (fp64.cu, pcg.cu): a value is h + l. Every add of leading parts is an exact
+// two-sum whose rounding error moves into l, every product takes the error of its leading
+// product from one fma (Dekker), and the l parts are carried with plain FP32 adds and never
+// renormalised. The leading parts are thus exact and the only rounding is that of the l chain,
+// about 2^-46 of the magnitudes that enter a butterfly or a row. Exact as long as no leading
+// part or rounding error falls below the FP32 normal range (|values| above about 1e-30).
+struct ddv {
+    float h, l;
+};
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ ddv dd_of(double v) {
+    const float h = __double2float_rn(v);
+    return ddv{h, __double2float_rn(v - (double)h)};
+}
+__device__ __forceinline__ double dd_value(ddv a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ ddv dd_add(ddv a, ddv b) {
+    float s, e;
+    two_sum(a.h, b.h, s, e);
+    return ddv{s, __fadd_rn(__fadd_rn(a.l, b.l), e)};
+}
+// (a, b) <- (a + b, b - a): one stage of the forward Walsh-Hadamard transform
+__device__ __forceinline__ void dd_fwd(ddv &a, ddv &b) {
+    float s, e, d, g;
+    two_sum(a.h, b.h, s, e);
+    two_sum(b.h, -a.h, d, g);
+    const ddv lo{s, __fadd_rn(__fadd_rn(a.l, b.l), e)};
+    b = ddv{d, __fadd_rn(__fsub_rn(b.l, a.l), g)};
+    a = lo;
+}
+// (a, b) <- (a - b, a + b): one stage of the inverse transform
+__device__ __forceinline__ void dd_inv(ddv &a, ddv &b) {
+    float s, e, d, g;
+    two_sum(a.h, -b.h, d, g);
+    two_sum(a.h, b.h, s, e);
+    const ddv hi{s, __fadd_rn(__fadd_rn(a.l, b.l), e)};
+    a = ddv{d, __fadd_rn(__fsub_rn(a.l, b.l), g)};
+    b = hi;
+}
+// (ch + cl) (q.h + q.l), the product of the low parts dropped
+__device__ __forceinline__ ddv dd_mul(float ch, float cl, ddv q) {
+    const float p = __fmul_rn(ch, q.h);
+    float e = __fmaf_rn(ch, q.h, -p);
+    e = __fmaf_rn(ch, q.l, e);
+    e = __fmaf_rn(cl, q.h, e);
+    return ddv{p, e};
+}
+
 constexpr int kModalNnz = 45;
 
 // Modal form of the isotropic cube element (see apply_modal.cuh). Sparsity pattern of Km in (mode*3 + component) indices (derived from the quadrature
@@ -277,6 +329,10 @@ struct ModalK {
 };
 struct ModalKD {
     double v[kModalNnz];
+};
+// The same as double-float pairs (h + l = the FP64 value to 2^-48).
+struct ModalKDD {
+    float h[kModalNnz], l[kModalNnz];
 };
 
 }  // namespace gbs

@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include "internal.h"
+#include "modal_dd.cuh"
 
 namespace gbs {
 
@@ -124,6 +125,38 @@ __global__ void __launch_bounds__(128) sens_kernel(int nx, int ny, int nz, Law<d
         if (dc) dc[e] = (float)(-dmodulus(law, xe) * s);
         if (ce_out) ce_out[e] = (float)s;
         part += modulus(law, xe) * s;
+    }
+    if (energy_out) {
+        const double v[1] = {part};
+        if (last_block_reduce<1>(v, partials, counter, tot, sred) && threadIdx.x == 0) *energy_out = tot[0];
+    }
+}
+
+// The same through the double-float modal form (modal_dd.cuh), from the split displacements:
+// ce = q^T Km q accumulated in double-float, then dc, ce and the energy partial as above.
+__global__ void __launch_bounds__(128) sens_dd_kernel(int nx, int ny, int nz, Law<double> law, const ModalKDD km,
+                                                      const float *__restrict__ x, const float2 *__restrict__ udd,
+                                                      float *dc, float *ce_out, double *partials, unsigned *counter,
+                                                      double *energy_out) {
+    __shared__ double sred[32];
+    __shared__ double tot[1];
+    const int64_t n_elem = (int64_t)nx * ny * nz;
+    double part = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_elem; e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e / ((int64_t)ny * nz)), j = (int)((e / nz) % ny), k = (int)(e % nz);
+        ddv q[8][3], r[8][3];
+        modal_fwd_dd(ny, nz, i, j, k, udd, q);
+        modal_km_dd(km, q, r);
+        ddv s{0.0f, 0.0f};
+#pragma unroll
+        for (int m = 1; m < 8; ++m)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) s = dd_add(s, dd_mul(q[m][c].h, q[m][c].l, r[m][c]));
+        const double ce = dd_value(s);
+        const double xe = (double)x[e];
+        if (dc) dc[e] = (float)(-dmodulus(law, xe) * ce);
+        if (ce_out) ce_out[e] = (float)ce;
+        part += modulus(law, xe) * ce;
     }
     if (energy_out) {
         const double v[1] = {part};
@@ -511,11 +544,11 @@ using namespace gbs;
 // ---- C ABI ------------------------------------------------------------------------------
 static size_t reduce_ws_bytes(int64_t nblocks) { return 256 + ((size_t)nblocks * 8 * 4 + 255) / 256 * 256; }
 
+// [counter][partials][the double-float split of u (modal Ke)]
 extern "C" size_t gbsimp_sensitivity_ws_bytes(int nx, int ny, int nz) {
-    (void)nx;
-    (void)ny;
-    (void)nz;
-    return reduce_ws_bytes(4096);
+    if (!grid_ok(nx, ny, nz)) return reduce_ws_bytes(4096);
+    const size_t nd = 3 * (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+    return reduce_ws_bytes(4096) + (nd * sizeof(float2) + 255) / 256 * 256;
 }
 
 extern "C" int gbsimp_sensitivity(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
@@ -523,7 +556,7 @@ extern "C" int gbsimp_sensitivity(gbsimp_ctx *ctx, int nx, int ny, int nz, const
                                   size_t ws_bytes, void *stream) {
     if (!ctx || !law || !x || !u || !grid_ok(nx, ny, nz))
         return set_error(GBS_EINVAL, "gbsimp_sensitivity: bad arguments");
-    if (energy_out && (!ws || ws_bytes < gbsimp_sensitivity_ws_bytes(nx, ny, nz)))
+    if (energy_out && (!ws || ws_bytes < reduce_ws_bytes(4096)))
         return set_error(GBS_EINVAL, "gbsimp_sensitivity: workspace too small");
     const int64_t n = (int64_t)nx * ny * nz;
     const unsigned blocks = reduce_blocks(ctx, n, 128);
@@ -531,6 +564,17 @@ extern "C" int gbsimp_sensitivity(gbsimp_ctx *ctx, int nx, int ny, int nz, const
     double *partials = (double *)((char *)ws + 256);
     cudaStream_t st = (cudaStream_t)stream;
     if (energy_out) GBS_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned), st));
+    // The double-float element products need the split of u in the workspace; without room
+    // for it (a workspace sized for the energy sum only, or none) the FP64 pass runs.
+    if (ctx->modal_ok && ws && ws_bytes >= gbsimp_sensitivity_ws_bytes(nx, ny, nz)) {
+        float2 *udd = (float2 *)((char *)ws + reduce_ws_bytes(4096));
+        int rc = split_dd(ctx, 3 * (int64_t)(nx + 1) * (ny + 1) * (nz + 1), u, nullptr, udd, st);
+        if (rc) return rc;
+        sens_dd_kernel<<<blocks, 128, 0, st>>>(nx, ny, nz, make_law<double>(*law), modal_kdd(ctx->kmd), x, udd, dc,
+                                               ce, partials, counter, energy_out);
+        GBS_LAUNCH_CHECK("sens_dd_kernel");
+        return GBS_OK;
+    }
     sens_kernel<<<blocks, 128, 0, st>>>(nx, ny, nz, make_law<double>(*law), ctx->ked, ctx->translation_free ? 1 : 0,
                                         ctx->modal_ok ? 1 : 0, ctx->kmd, x, u, dc, ce, partials, counter, energy_out);
     GBS_LAUNCH_CHECK("sens_kernel");

@@ -4,6 +4,7 @@
 // ~140-210 FP64 operations of the modal form per element replace 576 DFMA.
 #include "apply_modal.cuh"
 #include "internal.h"
+#include "modal_dd.cuh"
 
 namespace gbs {
 
@@ -119,6 +120,59 @@ int apply_f64_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_
     GBS_LAUNCH_CHECK("modal_elem64_kernel");
     gather64_kernel<<<b2, 256, 0, st>>>(nx, ny, nz, C, mask, y);
     GBS_LAUNCH_CHECK("gather64_kernel");
+    return GBS_OK;
+}
+
+// ---- double-float element products (the outer residual of defect correction) --------------
+// udd = the double-float split of u (h = u rounded to FP32, l = the rest rounded), fixed DOFs
+// zero when a mask is given.
+__global__ void split_dd_kernel(int64_t nd, const double *__restrict__ u, const uint8_t *__restrict__ mask,
+                                float2 *udd) {
+    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
+        const bool fx = mask && ((mask[d / 3] >> (int)(d % 3)) & 1);
+        const ddv v = fx ? ddv{0.0f, 0.0f} : dd_of(u[d]);
+        udd[d] = make_float2(v.h, v.l);
+    }
+}
+
+// Element pass: C[(b*3+c) * n_elem + e] = E_e (Ke u_e) at corner b, as (h, l) pairs.
+__global__ void __launch_bounds__(128) modal_elem_dd_kernel(int nx, int ny, int nz, Law<double> law,
+                                                            const ModalKDD km, const float *__restrict__ x,
+                                                            const float2 *__restrict__ udd, float2 *__restrict__ C) {
+    const int64_t n_elem = (int64_t)nx * ny * nz;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_elem; e += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e / ((int64_t)ny * nz)), j = (int)((e / nz) % ny), k = (int)(e % nz);
+        ddv v[8][3], r[8][3];
+        modal_fwd_dd(ny, nz, i, j, k, udd, v);
+        modal_km_dd(km, v, r);
+        const ddv E = dd_of(modulus(law, (double)x[e]));
+#pragma unroll
+        for (int m = 1; m < 8; ++m)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) r[m][c] = dd_mul(E.h, E.l, r[m][c]);
+        modal_inv_dd(r);
+#pragma unroll
+        for (int b = 0; b < 8; ++b)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) C[(b * 3 + c) * n_elem + e] = make_float2(r[b][c].h, r[b][c].l);
+    }
+}
+
+int split_dd(const gbsimp_ctx *ctx, int64_t nd, const double *u, const uint8_t *mask, float2 *udd, cudaStream_t st) {
+    int64_t b = (nd + 255) / 256;
+    const int64_t cap = 4LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+    split_dd_kernel<<<(unsigned)(b < cap ? (b < 1 ? 1 : b) : cap), 256, 0, st>>>(nd, u, mask, udd);
+    GBS_LAUNCH_CHECK("split_dd_kernel");
+    return GBS_OK;
+}
+
+int elem_dd_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
+                  const float2 *udd, float2 *C, cudaStream_t st) {
+    const int64_t ne = (int64_t)nx * ny * nz;
+    const int64_t cap = 32LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+    const unsigned b1 = (unsigned)((ne + 127) / 128 < cap ? (ne + 127) / 128 : cap);
+    modal_elem_dd_kernel<<<b1, 128, 0, st>>>(nx, ny, nz, make_law<double>(*law), modal_kdd(ctx->kmd), x, udd, C);
+    GBS_LAUNCH_CHECK("modal_elem_dd_kernel");
     return GBS_OK;
 }
 

@@ -30,6 +30,13 @@ int filter_launch(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, in
 size_t apply_f64_modal_ws_bytes(int nx, int ny, int nz);
 int apply_f64_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
                     const double *p, double *y, const uint8_t *mask, double *C, cudaStream_t st);
+// Double-float element products (modal_dd.cuh). split_dd: udd = (h, l) split of u, fixed DOFs
+// zero when mask is given. elem_dd_modal: the element pass of K(x) u from udd, corner
+// contributions to C as (h, l) pairs in the layout of apply_f64_modal (24 * n_elem float2).
+// Both require ctx->modal_ok for the element pass.
+int split_dd(const gbsimp_ctx *ctx, int64_t nd, const double *u, const uint8_t *mask, float2 *udd, cudaStream_t st);
+int elem_dd_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
+                  const float2 *udd, float2 *C, cudaStream_t st);
 // OC update with an explicit scratch pointer (layout of gbsimp_oc_ws_bytes).
 size_t oc_ws_bytes_impl(int64_t n_elem);
 // The filter row sums Hs inside an OC workspace (valid after oc_prepare_impl).

@@ -1073,13 +1073,14 @@ struct SolveWs {
     float *b32, *d32;
     double *partials;
     void *pcg;
-    double *elem;  // 24 * n_elem doubles for the modal FP64 residual
+    double *elem;  // 24 * n_elem corner contributions of the modal residual (FP64 or (h, l) float2)
+    float2 *udd;   // double-float split of u (double-float residual)
 };
 
 static size_t solve_ws_bytes_impl(int nx, int ny, int nz) {
     const size_t nd = (size_t)n_dof_of(nx, ny, nz);
     return 256 + al256(sizeof(OuterScalars)) + al256(nd * 8) + 2 * al256(nd * 4) + al256(3 * 4096 * 8) +
-           al256(pcg_ws_bytes_impl(nx, ny, nz)) + al256(apply_f64_modal_ws_bytes(nx, ny, nz));
+           al256(pcg_ws_bytes_impl(nx, ny, nz)) + al256(apply_f64_modal_ws_bytes(nx, ny, nz)) + al256(nd * 8);
 }
 
 static SolveWs solve_ws(void *ws, int nx, int ny, int nz) {
@@ -1097,9 +1098,19 @@ static SolveWs solve_ws(void *ws, int nx, int ny, int nz) {
     w.partials = (double *)p;
     p += al256(3 * 4096 * 8);
     w.pcg = p;
-    p += pcg_ws_bytes_impl(nx, ny, nz);
+    p += al256(pcg_ws_bytes_impl(nx, ny, nz));
     w.elem = (double *)p;
+    p += al256(apply_f64_modal_ws_bytes(nx, ny, nz));
+    w.udd = (float2 *)p;
     return w;
+}
+
+// The outer residual runs in double-float (modal_dd.cuh) for tolerances down to this one: its
+// rounding, measured at most 6.1e-13 ||f|| on converged fields (32x16x16, 64^3), stays three
+// orders of magnitude below. Tighter tolerances take the FP64 element pass.
+constexpr double kDdMinRtol = 1e-9;
+static bool use_dd_residual(const gbsimp_ctx *ctx, const gbsimp_solve_opts *o) {
+    return ctx->modal_ok && o->rtol >= kDdMinRtol;
 }
 
 // r = D f - q (q = D K D u); ||r||^2, ||D f||^2 -> os.
@@ -1122,6 +1133,62 @@ __global__ void resid64_kernel(int64_t nd, const double *__restrict__ f, const d
     }
 }
 
+// The node pass of the double-float residual: q_n = the (up to) 8 corner contributions of the
+// element pass summed in the fixed order b = 0..7 (double-float), then r = D(f - q) in FP64
+// and ||r||^2, ||D f||^2 -> os.
+__global__ void __launch_bounds__(256) resid_dd_kernel(int nx, int ny, int nz, const float2 *__restrict__ C,
+                                                       const uint8_t *__restrict__ mask, const double *__restrict__ f,
+                                                       double *r, double *partials, OuterScalars *os) {
+    const int64_t NY = ny + 1, NZ = nz + 1;
+    const int64_t n_nodes = (int64_t)(nx + 1) * NY * NZ;
+    const int64_t n_elem = (int64_t)nx * ny * nz;
+    double rr = 0.0, ff = 0.0;
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(n / (NY * NZ)), j = (int)((n / NZ) % NY), k = (int)(n % NZ);
+        ddv acc[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            const int ei = i - (b >> 2), ej = j - ((b >> 1) & 1), ek = k - (b & 1);
+            if (ei < 0 || ej < 0 || ek < 0 || ei >= nx || ej >= ny || ek >= nz) continue;
+            const int64_t e = ((int64_t)ei * ny + ej) * nz + ek;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float2 w = C[(b * 3 + c) * n_elem + e];
+                acc[c] = dd_add(acc[c], ddv{w.x, w.y});
+            }
+        }
+        const uint8_t m = mask ? mask[n] : (uint8_t)0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const bool fx = (m >> c) & 1;
+            const double fd = fx ? 0.0 : f[3 * n + c];
+            const double rd = fx ? 0.0 : fd - dd_value(acc[c]);
+            r[3 * n + c] = rd;
+            rr = fma(rd, rd, rr);
+            ff = fma(fd, fd, ff);
+        }
+    }
+    __shared__ double tot[3];
+    if (last_block3(rr, ff, 0.0, partials, &os->counter, tot) && threadIdx.x == 0) {
+        os->rr = tot[0];
+        os->ff = tot[1];
+        os->scale = tot[0] > 0.0 ? 1.0 / sqrt(tot[0]) : 0.0;
+    }
+}
+
+// u += d / scale (FP64), fixed DOFs zero, and its double-float split for the next residual.
+__global__ void correct_dd_kernel(int64_t nd, const float *__restrict__ d, const OuterScalars *os,
+                                  const uint8_t *__restrict__ mask, double *u, float2 *udd) {
+    const double s = os->scale > 0.0 ? 1.0 / os->scale : 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x) {
+        const bool fx = dof_fixed(mask, i);
+        const double v = fx ? 0.0 : fma((double)d[i], s, u[i]);
+        u[i] = v;
+        const ddv w = fx ? ddv{0.0f, 0.0f} : dd_of(v);
+        udd[i] = make_float2(w.h, w.l);
+    }
+}
+
 __global__ void scale_to_f32_kernel(int64_t nd, const double *__restrict__ r, const OuterScalars *os, float *b,
                                     float *d) {
     const double s = os->scale;
@@ -1136,6 +1203,43 @@ __global__ void correct64_kernel(int64_t nd, const float *__restrict__ d, const 
     const double s = os->scale > 0.0 ? 1.0 / os->scale : 0.0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x)
         u[i] = dof_fixed(mask, i) ? 0.0 : fma((double)d[i], s, u[i]);
+}
+
+// The outer residual of u into w.r64 and w.os: double-float element products (udd current) or
+// the FP64 element pass.
+static int outer_residual(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
+                          const double *f, const uint8_t *mask, const double *u, bool dd, const SolveWs &w,
+                          cudaStream_t st) {
+    const int64_t nd = n_dof_of(nx, ny, nz);
+    int rc;
+    if (dd) {
+        rc = elem_dd_modal(ctx, nx, ny, nz, law, x, w.udd, (float2 *)w.elem, st);
+        if (rc) return rc;
+        resid_dd_kernel<<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, (const float2 *)w.elem, mask, f, w.r64,
+                                                                  w.partials, w.os);
+        GBS_LAUNCH_CHECK("resid_dd_kernel");
+        return GBS_OK;
+    }
+    rc = ctx->modal_ok ? apply_f64_modal(ctx, nx, ny, nz, law, x, u, w.r64, mask, w.elem, st)
+                       : apply_f64(ctx, nx, ny, nz, law, x, u, w.r64, mask, st);
+    if (rc) return rc;
+    // resid64 reads q from r64 and overwrites it in place (element-wise, same index).
+    resid64_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, f, w.r64, mask, w.r64, w.partials, w.os);
+    GBS_LAUNCH_CHECK("resid64_kernel");
+    return GBS_OK;
+}
+
+// u += d / scale, and with the double-float residual the split of the new u.
+static int outer_correct(const gbsimp_ctx *ctx, int64_t nd, const uint8_t *mask, double *u, bool dd,
+                         const SolveWs &w, cudaStream_t st) {
+    if (dd) {
+        correct_dd_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.d32, w.os, mask, u, w.udd);
+        GBS_LAUNCH_CHECK("correct_dd_kernel");
+    } else {
+        correct64_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.d32, w.os, mask, u);
+        GBS_LAUNCH_CHECK("correct64_kernel");
+    }
+    return GBS_OK;
 }
 
 // One host read per defect-correction round: the outer scalars and, when a PCG ran since the
@@ -1171,13 +1275,14 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
     const bool async = !o->profile;
     const PcgScalars *pending = nullptr;
     const PcgWs pw = pcg_ws(w.pcg, nx, ny, nz);
-    for (;;) {
-        int rc = ctx->modal_ok ? apply_f64_modal(ctx, nx, ny, nz, law, x, u, w.r64, mask, w.elem, st)
-                               : apply_f64(ctx, nx, ny, nz, law, x, u, w.r64, mask, st);
+    const bool dd = use_dd_residual(ctx, o);
+    if (dd) {
+        int rc = split_dd(ctx, nd, u, mask, w.udd, st);
         if (rc) return rc;
-        // resid64 reads q from r64 and overwrites it in place (element-wise, same index).
-        resid64_kernel<<<vb, 256, 0, st>>>(nd, f, w.r64, mask, w.r64, w.partials, w.os);
-        GBS_LAUNCH_CHECK("resid64_kernel");
+    }
+    for (;;) {
+        int rc = outer_residual(ctx, nx, ny, nz, law, x, f, mask, u, dd, w, st);
+        if (rc) return rc;
         OuterScalars h;
         PcgScalars ps;
         rc = read_outer(w.os, &h, pending, &ps, st);
@@ -1227,8 +1332,8 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
                 if (ps.iter == 0) break;
             }
         }
-        correct64_kernel<<<vb, 256, 0, st>>>(nd, w.d32, w.os, mask, u);
-        GBS_LAUNCH_CHECK("correct64_kernel");
+        rc = outer_correct(ctx, nd, mask, u, dd, w, st);
+        if (rc) return rc;
         if (status != GBS_OK) break;
     }
     if (stats) {
@@ -1620,7 +1725,8 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
     const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-4;
     // iteration budget of the inner PCGs in this round (0: each runs to its tolerance)
     const int budget = o->check_every > 0 ? o->check_every : 0;
-    // act: every active item; res: those between inner solves, which get an FP64 residual
+    const bool dd = use_dd_residual(ctx, o);
+    // act: every active item; res: those between inner solves, which get an outer residual
     // (the others resume their paused inner PCG)
     std::vector<int> act, res;
     for (int i = 0; i < n; ++i)
@@ -1637,15 +1743,16 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
         const size_t m = std::min(res.size() - k, (size_t)(4096 / per));
         for (size_t j = 0; j < m; ++j) {
             gbsimp_batch_item &it = items[res[k + j]];
-            const int64_t nd = n_dof_of(it.nx, it.ny, it.nz);
             SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
-            if (it.stats.outer == 0) GBS_CUDA_TRY(cudaMemsetAsync(w.os, 0, sizeof(OuterScalars), st));
-            int rc = ctx->modal_ok ? apply_f64_modal(ctx, it.nx, it.ny, it.nz, glaw, it.x, it.u, w.r64, it.node_mask,
-                                                     w.elem, st)
-                                   : apply_f64(ctx, it.nx, it.ny, it.nz, glaw, it.x, it.u, w.r64, it.node_mask, st);
+            if (it.stats.outer == 0) {
+                GBS_CUDA_TRY(cudaMemsetAsync(w.os, 0, sizeof(OuterScalars), st));
+                if (dd) {
+                    int rc = split_dd(ctx, n_dof_of(it.nx, it.ny, it.nz), it.u, it.node_mask, w.udd, st);
+                    if (rc) return rc;
+                }
+            }
+            int rc = outer_residual(ctx, it.nx, it.ny, it.nz, glaw, it.x, it.f, it.node_mask, it.u, dd, w, st);
             if (rc) return rc;
-            resid64_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, it.f, w.r64, it.node_mask, w.r64, w.partials, w.os);
-            GBS_LAUNCH_CHECK("resid64_kernel");
             GBS_CUDA_TRY(cudaMemcpyAsync((char *)hp + j * per, w.os, per, cudaMemcpyDeviceToHost, st));
         }
         GBS_CUDA_TRY(cudaStreamSynchronize(st));
@@ -1810,10 +1917,9 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
                     continue;
                 }
             }
-            const int64_t nd = n_dof_of(it.nx, it.ny, it.nz);
             SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
-            correct64_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.d32, w.os, it.node_mask, it.u);
-            GBS_LAUNCH_CHECK("correct64_kernel");
+            int rc = outer_correct(ctx, n_dof_of(it.nx, it.ny, it.nz), it.node_mask, it.u, dd, w, st);
+            if (rc) return rc;
             if (it.stats.status != GBS_OK) it.state = 2;
         }
     }

@@ -274,6 +274,60 @@ def test_solve_refined_vs_oracle(eng, grid, case, law):
     np.testing.assert_allclose(ug, uref, rtol=0, atol=1e-5 * np.abs(uref).max())
 
 
+@pytest.mark.parametrize("grid,case", [((16, 16, 10), "top_patch"), ((48, 24, 24), "cantilever"),
+                                       ((64, 64, 64), "top_patch")])
+def test_double_float_residual_certifies_fp64(eng, grid, case):
+    """At rtol >= 1e-9 the outer residual's element products run in double-float: the relres
+    a solve reports agrees with the FP64 residual of the returned u (FP64 apply) to 1e-11."""
+    f, fixed, x = _problem(grid, case)
+    lw = L.make_law("modified", 3.0)
+    m = _cuda(bcs.node_mask(*grid, fixed))
+    xd = _cuda(x)
+    u = torch.zeros(n_dof(grid), dtype=torch.float64, device="cuda")
+    st = eng.solve(grid, lw, xd, _cuda(f), m, u, rtol=1e-8)
+    assert st["status"] == L.GBS_OK and st["relres"] <= 1e-8, st
+    y = eng.apply(grid, lw, xd, u, m)
+    fixed_dof = _cuda(bcs.dof_mask(*grid, fixed).astype(bool))
+    fd = _cuda(f)
+    r = torch.where(fixed_dof, 0.0, fd - y)
+    rel64 = (r.norm() / torch.where(fixed_dof, 0.0, fd).norm()).item()
+    assert abs(rel64 - st["relres"]) <= 1e-11, (rel64, st["relres"])
+
+
+@pytest.mark.parametrize("grid,case", [((12, 6, 6), "cantilever"), ((24, 12, 12), "top_patch")])
+@pytest.mark.parametrize("law", ["ref", "modified"])
+def test_sensitivity_double_float_vs_fp64(eng, grid, case, law):
+    """The double-float sensitivity (workspace with room for the split of u) against the FP64
+    pass (a workspace sized for the energy sum only) on a converged displacement: dc and ce
+    to FP32 rounding, the energy to 1e-10. The double-float modes carry about 2^-46 of the
+    element's displacement magnitudes, which exceed its strain modes by up to the grid length
+    (2e-12 relative energy difference measured on the 12x6x6 cantilever)."""
+    import ctypes as C
+
+    from genpipeline_gb300.engine import _p, _stream
+
+    f, fixed, x = _problem(grid, case)
+    lw = L.make_law(law, 3.0)
+    xd = _cuda(x)
+    u = torch.zeros(n_dof(grid), dtype=torch.float64, device="cuda")
+    eng.solve(grid, lw, xd, _cuda(f), _cuda(bcs.node_mask(*grid, fixed)), u, rtol=1e-8)
+    ne = int(np.prod(grid))
+    out = {}
+    for full in (True, False):
+        nb = eng.lib.gbsimp_sensitivity_ws_bytes(*grid) if full else 256 + 4096 * 32
+        ws = torch.empty(nb, dtype=torch.uint8, device="cuda")
+        dc = torch.empty(ne, dtype=torch.float32, device="cuda")
+        ce = torch.empty(ne, dtype=torch.float32, device="cuda")
+        en = torch.zeros((), dtype=torch.float64, device="cuda")
+        L.check(eng.lib.gbsimp_sensitivity(eng.ctx, *grid, C.byref(lw), _p(xd), _p(u), _p(dc), _p(ce), _p(en),
+                                           _p(ws), nb, _stream()))
+        out[full] = (dc.cpu().numpy(), ce.cpu().numpy(), en.item())
+    (dc1, ce1, e1), (dc0, ce0, e0) = out[True], out[False]
+    np.testing.assert_allclose(dc1, dc0, rtol=2e-7, atol=1e-9 * np.abs(dc0).max())
+    np.testing.assert_allclose(ce1, ce0, rtol=2e-7, atol=1e-9 * np.abs(ce0).max())
+    assert e1 == pytest.approx(e0, rel=1e-10)
+
+
 def test_device_loop_and_host_loop_agree_bitwise(eng):
     """The graph WHILE loop and the host-launched (profiled) loop run the same kernels in the
     same order: identical bits, identical iteration counts."""
