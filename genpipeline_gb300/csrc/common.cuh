@@ -221,6 +221,37 @@ __device__ __forceinline__ void block_sum_df(df32 (&v)[K], float2 *scratch) {
     }
 }
 
+// Division of a grid index n < 2^31 by a fixed divisor 1 <= d < 2^31 as a multiply-high, an add
+// and a shift (Granlund and Montgomery 1994, round-up method): with l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1, n / d = (umulhi(n, m) + n) >> l for every n < 2^32 when
+// the sum is formed in 33 bits; for n < 2^31 it fits in 32. Replaces the 64-bit divisions of
+// the element and node index decompositions, which compile to a long call sequence.
+struct FastDiv {
+    uint32_t d, m, l;
+};
+inline FastDiv fast_div(uint32_t d) {
+    uint32_t l = 0;
+    while (l < 31 && (1u << l) < d) ++l;
+    const uint64_t m = (((uint64_t)1 << 32) * (((uint64_t)1 << l) - d)) / d + 1;
+    return FastDiv{d, (uint32_t)m, l};
+}
+__host__ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+#ifdef __CUDA_ARCH__
+    return (__umulhi(n, f.m) + n) >> f.l;
+#else
+    return (uint32_t)((((uint64_t)n * f.m) >> 32) + n) >> f.l;
+#endif
+}
+// (i, j, k) of the row-major index n of an (a, b, c) box, k fastest: by = fast_div(b), bc = fast_div(c).
+__host__ __device__ __forceinline__ void unflatten3(uint32_t n, const FastDiv &fb, const FastDiv &fc, int &i, int &j,
+                                                    int &k) {
+    const uint32_t q = fdiv(n, fc);
+    k = (int)(n - q * fc.d);
+    const uint32_t p = fdiv(q, fb);
+    j = (int)(q - p * fb.d);
+    i = (int)p;
+}
+
 // Unnormalised double-float values for the element products of the outer residual and of the
 // sensitivities (fp64.cu, pcg.cu): a value is h + l. Every add of leading parts is an exact
 // two-sum whose rounding error moves into l, every product takes the error of its leading

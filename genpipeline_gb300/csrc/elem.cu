@@ -5,6 +5,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <atomic>
+
 #include "internal.h"
 #include "modal_dd.cuh"
 
@@ -135,6 +137,7 @@ __global__ void __launch_bounds__(128) sens_kernel(int nx, int ny, int nz, Law<d
 // The same through the double-float modal form (modal_dd.cuh), from the split displacements:
 // ce = q^T Km q accumulated in double-float, then dc, ce and the energy partial as above.
 __global__ void __launch_bounds__(128) sens_dd_kernel(int nx, int ny, int nz, Law<double> law, const ModalKDD km,
+                                                      const FastDiv fy, const FastDiv fz,
                                                       const float *__restrict__ x, const float2 *__restrict__ udd,
                                                       float *dc, float *ce_out, double *partials, unsigned *counter,
                                                       double *energy_out) {
@@ -143,7 +146,8 @@ __global__ void __launch_bounds__(128) sens_dd_kernel(int nx, int ny, int nz, La
     const int64_t n_elem = (int64_t)nx * ny * nz;
     double part = 0.0;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_elem; e += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(e / ((int64_t)ny * nz)), j = (int)((e / nz) % ny), k = (int)(e % nz);
+        int i, j, k;
+        unflatten3((uint32_t)e, fy, fz, i, j, k);
         ddv q[8][3], r[8][3];
         modal_fwd_dd(ny, nz, i, j, k, udd, q);
         modal_km_dd(km, q, r);
@@ -210,12 +214,14 @@ __device__ __forceinline__ void unpack_off(int o, int &di, int &dj, int &dk) {
 
 // mode 0: out = (sum w v) / hs[e] (hs nullable: computed);  mode 1: out = sum w v/hs[e2];
 // mode 2 (hs): out = sum w over in-bounds neighbours. preserved (mode 0): out = 1 there.
-__global__ void __launch_bounds__(256) filter_kernel(int nx, int ny, int nz, const Stencil st, int mode,
+__global__ void __launch_bounds__(256) filter_kernel(int nx, int ny, int nz, const FastDiv fy, const FastDiv fz,
+                                                     const Stencil st, int mode,
                                                      const float *__restrict__ hs, const float *__restrict__ in,
                                                      const uint8_t *__restrict__ preserved, float *out) {
     const int64_t n_elem = (int64_t)nx * ny * nz;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_elem; e += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(e / ((int64_t)ny * nz)), j = (int)((e / nz) % ny), k = (int)(e % nz);
+        int i, j, k;
+        unflatten3((uint32_t)e, fy, fz, i, j, k);
         // FP32 with compensated (Neumaier) summation in the fixed stencil order: error of a
         // few ulp whatever the stencil size (up to ~900 terms at rmin 6).
         float s = 0.0f, sc = 0.0f, ws = 0.0f, wc = 0.0f;
@@ -259,7 +265,8 @@ int filter_launch(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, in
     int rc = make_stencil(rmin, &s);
     if (rc) return rc;
     const int64_t n = (int64_t)nx * ny * nz;
-    filter_kernel<<<elem_blocks(ctx, n, 256), 256, 0, st>>>(nx, ny, nz, s, mode, hs, in, preserved, out);
+    filter_kernel<<<elem_blocks(ctx, n, 256), 256, 0, st>>>(nx, ny, nz, fast_div(ny), fast_div(nz), s, mode, hs, in,
+                                                            preserved, out);
     GBS_LAUNCH_CHECK("filter_kernel");
     return GBS_OK;
 }
@@ -269,6 +276,8 @@ struct OcScalars {
     double l1, l2, lfinal, npres;
     int steps, done;
     unsigned counter;
+    unsigned bar;  // grid barrier of oc_coop_kernel (monotonic within one call)
+    int status;    // GBS_ETIMEOUT when a barrier wait of oc_coop_kernel ran out
     int pad;
 };
 
@@ -345,6 +354,8 @@ __global__ void oc_init_kernel(int64_t n, const OcParams P, const float *__restr
                                OcScalars *sc) {
     sc->done = 0;  // every block writes the same values
     sc->steps = 0;
+    sc->bar = 0;
+    sc->status = 0;
     if (P.l2 >= 0.0) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             sc->l1 = P.l1;
@@ -517,6 +528,205 @@ __global__ void __launch_bounds__(kOcThreads) oc_multi_kernel(int64_t n, const O
     }
 }
 
+__device__ __forceinline__ unsigned long long oc_now_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// ---- multisection in one cooperative launch ----------------------------------------------
+// The rounds of oc_multi_kernel without a launch per round. In each round every block
+// evaluates the kOcNodes trial volumes on its elements and publishes its block sums (slot
+// round & 1: a block rewrites a slot only after every block has left the barrier that read it),
+// arrives on a monotonic counter and waits, bounded in time, for all blocks; then every block
+// sums all partials in block order and walks the tree itself, so that all blocks hold the same
+// (l1, l2, lfinal, steps, done) and no broadcast is needed. After the last round each block
+// writes xnew for its elements (oc_final_kernel's step). A wait that runs out sets
+// sc->status = GBS_ETIMEOUT and ends the rounds; the host reports it.
+__global__ void __launch_bounds__(kOcThreads) oc_coop_kernel(int64_t n, const OcParams P, const float *__restrict__ x,
+                                                             const float *__restrict__ dc,
+                                                             const uint8_t *__restrict__ pres,
+                                                             const float *__restrict__ w, float2 *partials,
+                                                             OcScalars *sc, float *xnew, unsigned long long wait_ns) {
+    __shared__ float s_sq[kOcNodes];
+    __shared__ bool s_stop[kOcNodes];
+    __shared__ double s_mid[kOcNodes];
+    __shared__ float s_part[kOcNodes][kOcThreads + 8];  // rows padded: conflict-free column sums
+    __shared__ double s_tot[kOcNodes];
+    __shared__ double s_l1, s_l2, s_lfinal;
+    __shared__ int s_steps, s_done, s_ok;
+    const int tid = threadIdx.x;
+    const int nblk = gridDim.x, bid = blockIdx.x;
+    if (tid == 0) {
+        s_l1 = sc->l1;
+        s_l2 = sc->l2;
+        s_lfinal = sc->lfinal;
+        s_steps = sc->steps;
+        s_done = sc->done;
+        s_ok = 1;
+    }
+    __syncthreads();
+    const float sfloor = sqrtf(P.sqrt_floor);
+    const double target = P.volfrac * (double)n - sc->npres;  // vol > volfrac <=> sum > target
+    // Rounds have two shapes. While l1 is still 0 the bisection's midpoints are l2/2, l2/4, ...
+    // for as long as every volume stays at or below the target (each step sets l2 = mid); a
+    // chain round evaluates the next kOcNodes midpoints of that all-left path, formed exactly
+    // as bisection forms them (0.5 (hi + 0)), and ends at the first step that goes right. Once
+    // l1 > 0, tree rounds evaluate the full kOcLevels-level tree. Each round advances the
+    // bisection by at least one step, so max_bisect rounds bound the loop.
+    for (int round = 0; round < P.max_bisect; ++round) {
+        if (s_done || !s_ok) break;  // block-uniform: written before the last __syncthreads
+        const bool chain = s_l1 == 0.0;
+        if (tid < kOcNodes) {
+            double lo = s_l1, hi = s_l2;
+            if (chain) {
+                for (int i = 0; i < tid; ++i) hi = 0.5 * (hi + lo);
+            } else {
+                const int path = tid + 1, depth = 31 - __clz(path);
+                for (int i = depth - 1; i >= 0; --i) {
+                    const double m = 0.5 * (hi + lo);
+                    if ((path >> i) & 1)
+                        lo = m;
+                    else
+                        hi = m;
+                }
+            }
+            const double m = 0.5 * (hi + lo);
+            s_mid[tid] = m;
+            s_sq[tid] = (float)sqrt(1.0 / m);
+            s_stop[tid] = (hi - lo) / (lo + hi + P.tol_eps) < P.tol;
+        }
+        __syncthreads();
+        float sq[kOcNodes], v[kOcNodes];
+#pragma unroll
+        for (int t = 0; t < kOcNodes; ++t) {
+            sq[t] = s_sq[t];
+            v[t] = 0.0f;
+        }
+        for (int64_t e = bid * (int64_t)kOcThreads + tid; e < n; e += (int64_t)nblk * kOcThreads) {
+            const float we = w[e];
+            if (pres && pres[e]) {
+#pragma unroll
+                for (int t = 0; t < kOcNodes; ++t) v[t] += we;
+                continue;
+            }
+            const float xe = x[e], s0 = sqrtf(fmaxf(-dc[e], 0.0f));
+            const float lo = xe - P.move, hi = xe + P.move;
+#pragma unroll
+            for (int t = 0; t < kOcNodes; ++t) {
+                float tv = xe * fmaxf(s0 * sq[t], sfloor);
+                tv = fminf(fmaxf(tv, 0.0f), 1.0f);
+                tv = fminf(fmaxf(tv, lo), hi);
+                v[t] = fmaf(we, tv, v[t]);
+            }
+        }
+#pragma unroll
+        for (int t = 0; t < kOcNodes; ++t) s_part[t][tid] = v[t];
+        __syncthreads();
+        // block sums: node t = tid / 8 summed by the 8 lanes tid % 8 (columns sub, sub + 8, ...),
+        // then across those lanes; every sum in a fixed order
+        float2 *part = partials + (size_t)(round & 1) * kOcNodes * nblk;
+        const int t8 = tid >> 3, sub = tid & 7;
+        {
+            df32 a{0.0f, 0.0f};
+            if (t8 < kOcNodes)
+#pragma unroll 8
+                for (int j = sub; j < kOcThreads; j += 8) a = df_add(a, df32{s_part[t8][j], 0.0f});
+#pragma unroll
+            for (int o = 4; o > 0; o >>= 1)
+                a = df_add(a, df32{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)});
+            if (t8 < kOcNodes && sub == 0) part[t8 * nblk + bid] = make_float2(a.hi, a.lo);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            atomicAdd(&sc->bar, 1u);
+            const unsigned goal = (unsigned)nblk * (unsigned)(round + 1);
+            const unsigned long long t0 = oc_now_ns();
+            while (*(volatile unsigned *)&sc->bar < goal) {
+                if (oc_now_ns() - t0 > wait_ns) {
+                    s_ok = 0;
+                    atomicExch(&sc->status, (int)GBS_ETIMEOUT);
+                    break;
+                }
+                __nanosleep(64);
+            }
+            __threadfence();
+        }
+        __syncthreads();
+        if (!s_ok) break;
+        // totals, the same way over the blocks' partials (loads issued four at a time)
+        {
+            df32 a{0.0f, 0.0f};
+            if (t8 < kOcNodes) {
+                const float2 *pt = part + t8 * nblk;
+                int b = sub;
+                for (; b + 24 < nblk; b += 32) {
+                    const float2 p0 = __ldcg(&pt[b]), p1 = __ldcg(&pt[b + 8]), p2 = __ldcg(&pt[b + 16]),
+                                 p3 = __ldcg(&pt[b + 24]);
+                    a = df_add(a, df32{p0.x, p0.y});
+                    a = df_add(a, df32{p1.x, p1.y});
+                    a = df_add(a, df32{p2.x, p2.y});
+                    a = df_add(a, df32{p3.x, p3.y});
+                }
+                for (; b < nblk; b += 8) {
+                    const float2 p = __ldcg(&pt[b]);
+                    a = df_add(a, df32{p.x, p.y});
+                }
+            }
+#pragma unroll
+            for (int o = 4; o > 0; o >>= 1)
+                a = df_add(a, df32{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)});
+            if (t8 < kOcNodes && sub == 0) s_tot[t8] = df_value(a);
+        }
+        __syncthreads();
+        if (tid == 0) {  // bisection's tests along the chain or the tree (oc_multi_kernel's walk)
+            double l1 = s_l1, l2 = s_l2, lfinal = s_lfinal;
+            int steps = s_steps, done = 0, node = 0;
+            for (int lvl = 0; lvl < (chain ? kOcNodes : kOcLevels); ++lvl) {
+                const double m = s_mid[node];
+                if (s_stop[node]) {
+                    lfinal = m;
+                    steps += 1;
+                    done = 1;
+                    break;
+                }
+                const bool right = s_tot[node] > target;
+                if (right) {
+                    l1 = m;
+                    node = 2 * node + 2;
+                } else {
+                    l2 = m;
+                    node = chain ? node + 1 : 2 * node + 1;
+                }
+                lfinal = m;
+                steps += 1;
+                if (steps >= P.max_bisect) {
+                    done = 1;
+                    break;
+                }
+                if (chain && right) break;  // off the all-left path: tree rounds from here
+            }
+            s_l1 = l1;
+            s_l2 = l2;
+            s_lfinal = lfinal;
+            s_steps = steps;
+            s_done = done;
+        }
+        __syncthreads();
+    }
+    if (bid == 0 && tid == 0) {
+        sc->l1 = s_l1;
+        sc->l2 = s_l2;
+        sc->lfinal = s_lfinal;
+        sc->steps = s_steps;
+        sc->done = s_done;
+    }
+    const float inv_l = (float)(1.0 / s_lfinal);
+    for (int64_t e = bid * (int64_t)kOcThreads + tid; e < n; e += (int64_t)nblk * kOcThreads)
+        xnew[e] = oc_trial(x[e], dc[e], inv_l, P, pres && pres[e]);
+}
+
 __global__ void oc_final_kernel(int64_t n, const OcParams P, const float *__restrict__ x,
                                 const float *__restrict__ dc, const uint8_t *__restrict__ pres, const OcScalars *sc,
                                 float *xnew) {
@@ -570,7 +780,8 @@ extern "C" int gbsimp_sensitivity(gbsimp_ctx *ctx, int nx, int ny, int nz, const
         float2 *udd = (float2 *)((char *)ws + reduce_ws_bytes(4096));
         int rc = split_dd(ctx, 3 * (int64_t)(nx + 1) * (ny + 1) * (nz + 1), u, nullptr, udd, st);
         if (rc) return rc;
-        sens_dd_kernel<<<blocks, 128, 0, st>>>(nx, ny, nz, make_law<double>(*law), modal_kdd(ctx->kmd), x, udd, dc,
+        sens_dd_kernel<<<blocks, 128, 0, st>>>(nx, ny, nz, make_law<double>(*law), modal_kdd(ctx->kmd),
+                                               fast_div(ny), fast_div(nz), x, udd, dc,
                                                ce, partials, counter, energy_out);
         GBS_LAUNCH_CHECK("sens_dd_kernel");
         return GBS_OK;
@@ -617,6 +828,29 @@ int oc_prepare_impl(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, 
     return GBS_OK;
 }
 
+// Blocks of oc_coop_kernel that can be resident together on the context's device (cached per
+// device), capped by the partials room; 0 when cooperative launches are unavailable.
+static int oc_coop_blocks(const gbsimp_ctx *ctx) {
+    static std::atomic<int> cache[64];
+    const int dev = ctx->device;
+    if (dev < 0 || dev >= 64) return 0;
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v != 0) return v > 0 ? v : 0;
+    int coop = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, oc_coop_kernel, kOcThreads, 0) != cudaSuccess ||
+        per_sm < 1) {
+        (void)cudaGetLastError();
+        cache[dev].store(-1, std::memory_order_relaxed);
+        return 0;
+    }
+    constexpr int kRoom = (4 * 4096 * (int)sizeof(double)) / (2 * kOcNodes * (int)sizeof(float2));
+    v = per_sm * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+    v = v < kRoom ? v : kRoom;
+    cache[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
+
 int oc_run_impl(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const gbsimp_oc_params *prm, const float *x,
                 const float *dc, const uint8_t *preserved, float *xnew, float *xphys, void *ws, cudaStream_t st) {
     const int64_t n = (int64_t)nx * ny * nz;
@@ -633,6 +867,21 @@ int oc_run_impl(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, cons
     const unsigned blocks = reduce_blocks(ctx, n, 256);
     oc_init_kernel<<<blocks, 256, 0, st>>>(n, P, dc, w.partials, w.sc);
     GBS_LAUNCH_CHECK("oc_init_kernel");
+    // One cooperative launch for the multisection and xnew when its blocks can be resident
+    // together (two slots of kOcNodes double-float partials per block fit the workspace).
+    const int cb = oc_coop_blocks(ctx);
+    if (cb > 0) {
+        int64_t nb = (n + kOcThreads - 1) / kOcThreads;
+        nb = nb > cb ? cb : (nb < 1 ? 1 : nb);
+        float2 *parts = (float2 *)w.partials;
+        unsigned long long wait_ns = 2000000000ull;  // 2 s per barrier wait
+        void *args[] = {(void *)&n, (void *)&P, (void *)&x, (void *)&dc, (void *)&preserved, (void *)&w.w,
+                        (void *)&parts, (void *)&w.sc, (void *)&xnew, (void *)&wait_ns};
+        GBS_CUDA_TRY(cudaLaunchCooperativeKernel((void *)oc_coop_kernel, dim3((unsigned)nb), dim3(kOcThreads), args, 0,
+                                                 st));
+        GBS_LAUNCH_CHECK("oc_coop_kernel");
+        return filter_launch(ctx, nx, ny, nz, rmin, 0, w.hs, xnew, preserved, xphys, st);
+    }
     // kOcNodes double-float partials per block fit the 4 * 4096 doubles of the workspace
     int64_t mb = (n + kOcThreads - 1) / kOcThreads;
     const int64_t mcap = 2LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
@@ -686,6 +935,8 @@ extern "C" int gbsimp_oc_result(gbsimp_ctx *ctx, const void *ws, double *lambda_
     memcpy(&h, hp, sizeof h);
     if (lambda_out) *lambda_out = h.lfinal;
     if (steps_out) *steps_out = h.steps;
+    if (h.status == GBS_ETIMEOUT)
+        return set_error(GBS_ETIMEOUT, "gbsimp_oc_result: a grid barrier wait of the OC update ran out");
     return GBS_OK;
 }
 

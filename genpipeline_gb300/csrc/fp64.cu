@@ -137,11 +137,13 @@ __global__ void split_dd_kernel(int64_t nd, const double *__restrict__ u, const 
 
 // Element pass: C[(b*3+c) * n_elem + e] = E_e (Ke u_e) at corner b, as (h, l) pairs.
 __global__ void __launch_bounds__(128) modal_elem_dd_kernel(int nx, int ny, int nz, Law<double> law,
-                                                            const ModalKDD km, const float *__restrict__ x,
+                                                            const ModalKDD km, const FastDiv fy, const FastDiv fz,
+                                                            const float *__restrict__ x,
                                                             const float2 *__restrict__ udd, float2 *__restrict__ C) {
     const int64_t n_elem = (int64_t)nx * ny * nz;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n_elem; e += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(e / ((int64_t)ny * nz)), j = (int)((e / nz) % ny), k = (int)(e % nz);
+        int i, j, k;
+        unflatten3((uint32_t)e, fy, fz, i, j, k);
         ddv v[8][3], r[8][3];
         modal_fwd_dd(ny, nz, i, j, k, udd, v);
         modal_km_dd(km, v, r);
@@ -171,7 +173,8 @@ int elem_dd_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_la
     const int64_t ne = (int64_t)nx * ny * nz;
     const int64_t cap = 32LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
     const unsigned b1 = (unsigned)((ne + 127) / 128 < cap ? (ne + 127) / 128 : cap);
-    modal_elem_dd_kernel<<<b1, 128, 0, st>>>(nx, ny, nz, make_law<double>(*law), modal_kdd(ctx->kmd), x, udd, C);
+    modal_elem_dd_kernel<<<b1, 128, 0, st>>>(nx, ny, nz, make_law<double>(*law), modal_kdd(ctx->kmd), fast_div(ny),
+                                             fast_div(nz), x, udd, C);
     GBS_LAUNCH_CHECK("modal_elem_dd_kernel");
     return GBS_OK;
 }

@@ -136,12 +136,13 @@ __device__ __forceinline__ bool dof_fixed(const uint8_t *mask, int64_t d) {
 
 // dinv = 1 / diag(K(x)) on free DOFs, 0 on fixed DOFs; diag_{n,c} = sum_{e ∋ n} E_e Ke[(a,c),(a,c)].
 template <typename T>
-__global__ void dinv_kernel(int nx, int ny, int nz, Law<T> law, const KeF kd, const float *__restrict__ x,
-                            const uint8_t *__restrict__ mask, float *dinv) {
+__global__ void dinv_kernel(int nx, int ny, int nz, const FastDiv fNY, const FastDiv fNZ, Law<T> law, const KeF kd,
+                            const float *__restrict__ x, const uint8_t *__restrict__ mask, float *dinv) {
     const int64_t NY = ny + 1, NZ = nz + 1;
     const int64_t n_nodes = (int64_t)(nx + 1) * NY * NZ;
     for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(n / (NY * NZ)), j = (int)((n / NZ) % NY), k = (int)(n % NZ);
+        int i, j, k;
+        unflatten3((uint32_t)n, fNY, fNZ, i, j, k);
         T acc[3] = {0, 0, 0};
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
@@ -153,7 +154,8 @@ __global__ void dinv_kernel(int nx, int ny, int nz, Law<T> law, const KeF kd, co
         }
         const uint8_t m = mask ? mask[n] : (uint8_t)0;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) dinv[3 * n + c] = ((m >> c) & 1) || !(acc[c] > 0) ? 0.0f : (float)(1.0 / (double)acc[c]);
+        for (int c = 0; c < 3; ++c)
+            dinv[3 * n + c] = ((m >> c) & 1) || !(acc[c] > 0) ? 0.0f : (float)((T)1 / acc[c]);
     }
 }
 
@@ -912,7 +914,8 @@ static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp
     }
     GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
     if (!(flags & SETUP_KEEP_DINV)) {
-        dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, law, ctx->kef, x, mask, w.dinv);
+        dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, fast_div(ny + 1), fast_div(nz + 1), law,
+                                                                     ctx->kef, x, mask, w.dinv);
         GBS_LAUNCH_CHECK("dinv_kernel");
         if (use_modal(ctx, nz)) {
             const int64_t ne = (int64_t)nx * ny * nz;
@@ -1136,7 +1139,8 @@ __global__ void resid64_kernel(int64_t nd, const double *__restrict__ f, const d
 // The node pass of the double-float residual: q_n = the (up to) 8 corner contributions of the
 // element pass summed in the fixed order b = 0..7 (double-float), then r = D(f - q) in FP64
 // and ||r||^2, ||D f||^2 -> os.
-__global__ void __launch_bounds__(256) resid_dd_kernel(int nx, int ny, int nz, const float2 *__restrict__ C,
+__global__ void __launch_bounds__(256) resid_dd_kernel(int nx, int ny, int nz, const FastDiv fNY, const FastDiv fNZ,
+                                                       const float2 *__restrict__ C,
                                                        const uint8_t *__restrict__ mask, const double *__restrict__ f,
                                                        double *r, double *partials, OuterScalars *os) {
     const int64_t NY = ny + 1, NZ = nz + 1;
@@ -1144,7 +1148,8 @@ __global__ void __launch_bounds__(256) resid_dd_kernel(int nx, int ny, int nz, c
     const int64_t n_elem = (int64_t)nx * ny * nz;
     double rr = 0.0, ff = 0.0;
     for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(n / (NY * NZ)), j = (int)((n / NZ) % NY), k = (int)(n % NZ);
+        int i, j, k;
+        unflatten3((uint32_t)n, fNY, fNZ, i, j, k);
         ddv acc[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
 #pragma unroll
         for (int b = 0; b < 8; ++b) {
@@ -1215,7 +1220,8 @@ static int outer_residual(const gbsimp_ctx *ctx, int nx, int ny, int nz, const g
     if (dd) {
         rc = elem_dd_modal(ctx, nx, ny, nz, law, x, w.udd, (float2 *)w.elem, st);
         if (rc) return rc;
-        resid_dd_kernel<<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, (const float2 *)w.elem, mask, f, w.r64,
+        resid_dd_kernel<<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, fast_div(ny + 1), fast_div(nz + 1),
+                                                                  (const float2 *)w.elem, mask, f, w.r64,
                                                                   w.partials, w.os);
         GBS_LAUNCH_CHECK("resid_dd_kernel");
         return GBS_OK;
@@ -1533,7 +1539,8 @@ extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, co
         if (rc) return rc;
     }
     GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
-    dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, law, ctx->kef, x, node_mask, w.dinv);
+    dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, fast_div(ny + 1), fast_div(nz + 1), law,
+                                                                 ctx->kef, x, node_mask, w.dinv);
     fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 1.0f, w.r);
     fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.p1);
     fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, xu);
