@@ -272,6 +272,35 @@ __device__ __forceinline__ ddv dd_of(double v) {
     return ddv{h, __double2float_rn(v - (double)h)};
 }
 __device__ __forceinline__ double dd_value(ddv a) { return (double)a.h + (double)a.l; }
+// (double)x from the bits of a normal FP32 x (exponent rebiased, mantissa widened); zero,
+// subnormals, infinities and NaN take the conversion instruction.
+__device__ __forceinline__ double f2d(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (b & 0x7fffffffu) == 0u ? (b ? -0.0 : 0.0) : (double)x;
+    return __longlong_as_double((long long)(((unsigned long long)(b >> 31) << 63) |
+                                            ((unsigned long long)(e + 896u) << 52) |
+                                            ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+// dd_of(v) from the bits of v with integer operations, off the FP64 pipe (whose conversions
+// run far below its add rate on this part): h = v rounded to 24 bits (nearest, ties to even)
+// as an integer add on the bit pattern, v - h = (bits(v) - bits(h)) units of 2^(e - 1075) (the
+// difference of the patterns counts mantissa units across a binade carry too), rounded to
+// FP32 by the integer conversion and scaled exactly. Values with |v| outside [2^-70, 2^100],
+// and zero, subnormals, infinities and NaN, take dd_of.
+__device__ __forceinline__ ddv dd_split(double v) {
+    const long long b = __double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e < 1023 - 70 || e > 1023 + 100) return dd_of(v);
+    const long long rb = (b + ((1LL << 28) - 1) + ((b >> 29) & 1)) & ~((1LL << 29) - 1);
+    const int eh = (int)((rb >> 52) & 0x7ff);
+    const unsigned sign = (unsigned)((unsigned long long)b >> 63) << 31;
+    const float h = __uint_as_float(sign | ((unsigned)(eh - 1023 + 127) << 23) | (unsigned)((rb >> 29) & 0x7fffff));
+    const int d = (int)(b - rb);  // |d| <= 2^28: the remainder in units of 2^(e - 1075), sign of |v| - |h|
+    const float scale = __uint_as_float((unsigned)(e - 1075 + 127) << 23);
+    const float l = __fmul_rn(__int2float_rn(d), scale);
+    return ddv{h, sign ? -l : l};
+}
 __device__ __forceinline__ ddv dd_add(ddv a, ddv b) {
     float s, e;
     two_sum(a.h, b.h, s, e);

@@ -130,13 +130,13 @@ __global__ void split_dd_kernel(int64_t nd, const double *__restrict__ u, const 
                                 float2 *udd) {
     for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
         const bool fx = mask && ((mask[d / 3] >> (int)(d % 3)) & 1);
-        const ddv v = fx ? ddv{0.0f, 0.0f} : dd_of(u[d]);
+        const ddv v = fx ? ddv{0.0f, 0.0f} : dd_split(u[d]);
         udd[d] = make_float2(v.h, v.l);
     }
 }
 
 // Element pass: C[(b*3+c) * n_elem + e] = E_e (Ke u_e) at corner b, as (h, l) pairs.
-__global__ void __launch_bounds__(128) modal_elem_dd_kernel(int nx, int ny, int nz, Law<double> law,
+__global__ void __launch_bounds__(128) modal_elem_dd_kernel(int nx, int ny, int nz, const LawDD law,
                                                             const ModalKDD km, const FastDiv fy, const FastDiv fz,
                                                             const float *__restrict__ x,
                                                             const float2 *__restrict__ udd, float2 *__restrict__ C) {
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(128) modal_elem_dd_kernel(int nx, int ny, int 
         ddv v[8][3], r[8][3];
         modal_fwd_dd(ny, nz, i, j, k, udd, v);
         modal_km_dd(km, v, r);
-        const ddv E = dd_of(modulus(law, (double)x[e]));
+        const ddv E = modulus_dd(law, x[e]);
 #pragma unroll
         for (int m = 1; m < 8; ++m)
 #pragma unroll
@@ -173,7 +173,7 @@ int elem_dd_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_la
     const int64_t ne = (int64_t)nx * ny * nz;
     const int64_t cap = 32LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
     const unsigned b1 = (unsigned)((ne + 127) / 128 < cap ? (ne + 127) / 128 : cap);
-    modal_elem_dd_kernel<<<b1, 128, 0, st>>>(nx, ny, nz, make_law<double>(*law), modal_kdd(ctx->kmd), fast_div(ny),
+    modal_elem_dd_kernel<<<b1, 128, 0, st>>>(nx, ny, nz, make_law_dd(*law), modal_kdd(ctx->kmd), fast_div(ny),
                                              fast_div(nz), x, udd, C);
     GBS_LAUNCH_CHECK("modal_elem_dd_kernel");
     return GBS_OK;

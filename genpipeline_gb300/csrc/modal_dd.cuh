@@ -18,6 +18,42 @@ inline ModalKDD modal_kdd(const ModalKD &k) {
     return d;
 }
 
+// The stiffness law for double-float element moduli: e0, emin, e0 - emin and xmin as (h, l)
+// pairs of their FP64 values, and the FP64 law for penalties that are not small integers.
+struct LawDD {
+    int kind, pint;
+    ddv e0, emin, span, xmin;
+    Law<double> law;
+};
+inline ddv dd_host(double v) {
+    const float h = (float)v;
+    return ddv{h, (float)(v - (double)h)};
+}
+inline LawDD make_law_dd(const gbsimp_law &l) {
+    LawDD d;
+    d.law = make_law<double>(l);
+    d.kind = d.law.kind;
+    d.pint = d.law.pint;
+    d.e0 = dd_host(l.e0);
+    d.emin = dd_host(l.emin);
+    d.span = dd_host(l.e0 - l.emin);
+    d.xmin = dd_host(l.xmin);
+    return d;
+}
+
+// E(x) of modulus() in double-float from an FP32 density: x^p by exact first product and
+// double-float products after it (integer p <= 4), the law's constants as pairs; about 2^-48
+// relative. Other penalties: the FP64 law, split.
+__device__ __forceinline__ ddv modulus_dd(const LawDD &L, float x) {
+    if (L.pint < 0) return dd_split(modulus(L.law, (double)x));
+    ddv base{x, 0.0f};
+    if (L.kind == 0 && !(x > L.xmin.h || (x == L.xmin.h && L.xmin.l < 0.0f))) base = L.xmin;  // max(x, xmin)
+    ddv p{1.0f, 0.0f};
+    for (int i = 0; i < L.pint; ++i) p = i == 0 ? base : dd_mul(base.h, base.l, p);
+    if (L.kind == 0) return dd_mul(L.e0.h, L.e0.l, p);
+    return dd_add(L.emin, dd_mul(L.span.h, L.span.l, p));
+}
+
 // q = T^T u_e of element (i, j, k): corners in bit order (x, y, z) = (4, 2, 1), from the
 // split displacements udd (h, l per DOF).
 __device__ __forceinline__ void modal_fwd_dd(int ny, int nz, int i, int j, int k, const float2 *__restrict__ udd,

@@ -187,6 +187,40 @@ __device__ bool last_block3(double a, double b, double c, double *partials, unsi
     return true;
 }
 
+// The same for FP32 per-thread partials, in double-float on the FP32 pipe (block sums, the
+// per-block partials and the last block's sum in block order); the totals in out[] are valid
+// in thread 0 of the last block.
+__device__ bool last_block3_df(float a, float b, float c, float2 *partials, unsigned *counter, double *out) {
+    __shared__ float2 sred[3 * 32];
+    __shared__ bool last;
+    const int nblk = gridDim.x;
+    df32 v[3] = {{a, 0.0f}, {b, 0.0f}, {c, 0.0f}};
+    block_sum_df<3>(v, sred);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) partials[k * nblk + blockIdx.x] = make_float2(v[k].hi, v[k].lo);
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == (unsigned)(nblk - 1));
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    df32 s[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+    for (int i = threadIdx.x; i < nblk; i += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float2 p = __ldcg(&partials[k * nblk + i]);
+            s[k] = df_add(s[k], df32{p.x, p.y});
+        }
+    block_sum_df<3>(s, sred);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) out[k] = df_value(s[k]);
+        *counter = 0;
+    }
+    return true;
+}
+
 // r = D b - q (q = D K D x0), x0 fixed entries zeroed, p_{-1} = 0; sums r.z, r.r, (Db).(Db).
 __global__ void pcg_init_kernel(int64_t nd, const float *__restrict__ b, const float *__restrict__ q,
                                 const uint8_t *__restrict__ mask, const float *__restrict__ dinv, float *r, float *pprev,
@@ -229,26 +263,28 @@ __global__ void pcg_init_kernel(int64_t nd, const float *__restrict__ b, const f
 // Single-reduction setup, step 1: r_0 = D b - q (q = D K D x0, read from `qu`), u_0 = M r_0
 // written over q, p_{-1} = s_{-1} = 0, fixed entries of x0 zeroed; sums r.u, r.r, (Db).(Db)
 // and the stop test of the initial guess.
+// x0_zero: x0 = 0 is known, q is not read (and x0 is written as zero).
 __global__ void cg_init_kernel(int64_t nd, const float *__restrict__ b, float *qu, const uint8_t *__restrict__ mask,
                                const float *__restrict__ dinv, float *r, float *p, float *sprev, float *xu,
-                               double *partials, PcgScalars *sc, double tol, int max_iter, int max_trips) {
+                               double *partials, PcgScalars *sc, double tol, int max_iter, int max_trips,
+                               int x0_zero) {
     float ru = 0.0f, rr = 0.0f, bb = 0.0f;
     for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
         const bool fx = dof_fixed(mask, d);
         const float bd = fx ? 0.0f : b[d];
-        const float rd = fx ? 0.0f : bd - qu[d];
+        const float rd = fx ? 0.0f : (x0_zero ? bd : bd - qu[d]);
         const float ud = dinv[d] * rd;
         r[d] = rd;
         qu[d] = ud;
         p[d] = 0.0f;
         sprev[d] = 0.0f;
-        if (fx) xu[d] = 0.0f;
+        if (fx || x0_zero) xu[d] = 0.0f;
         ru = fmaf(rd, ud, ru);
         rr = fmaf(rd, rd, rr);
         bb = fmaf(bd, bd, bb);
     }
     __shared__ double tot[3];
-    if (last_block3(ru, rr, bb, partials, &sc->counter, tot) && threadIdx.x == 0) {
+    if (last_block3_df(ru, rr, bb, (float2 *)partials, &sc->counter, tot) && threadIdx.x == 0) {
         sc->rz = tot[0];
         sc->rr = tot[1];
         sc->bnorm = sqrt(tot[2]);
@@ -288,7 +324,7 @@ __global__ void cg_start_kernel(int64_t nd, const float *__restrict__ w, const f
     for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x)
         wu = fmaf(w[d], u[d], wu);
     __shared__ double tot[3];
-    if (last_block3(wu, 0.0, 0.0, partials, &sc->counter, tot) && threadIdx.x == 0) {
+    if (last_block3_df(wu, 0.0f, 0.0f, (float2 *)partials, &sc->counter, tot) && threadIdx.x == 0) {
         sc->pap = tot[0];
         if (!isfinite(tot[0])) {
             sc->done = 1;
@@ -934,12 +970,15 @@ static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp
     };
     if (use_modal(ctx, nz)) {
         const CgArgs ca = cg_args(w, u);
-        int rc = start_q(ca.w[1]);
-        if (rc) return rc;
+        const int x0_zero = (flags & SETUP_X0_ZERO) ? 1 : 0;
+        if (!x0_zero) {
+            const int rc = start_q(ca.w[1]);
+            if (rc) return rc;
+        }
         cg_init_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, b, ca.w[1], mask, w.dinv, ca.r[0], ca.p, ca.s[1], u,
-                                                           w.partials, w.sc, rtol, max_iter, max_trips);
+                                                           w.partials, w.sc, rtol, max_iter, max_trips, x0_zero);
         GBS_LAUNCH_CHECK("cg_init_kernel");
-        rc = apply_f32(ctx, nx, ny, nz, glaw, x, ca.w[1], ca.w[0], mask, st);
+        int rc = apply_f32(ctx, nx, ny, nz, glaw, x, ca.w[1], ca.w[0], mask, st);
         if (rc) return rc;
         cg_start_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, ca.w[0], ca.w[1], w.partials, w.sc);
         GBS_LAUNCH_CHECK("cg_start_kernel");
@@ -1066,8 +1105,10 @@ struct OuterScalars {
     double ff;      // ||D f||^2
     double rr;      // ||D(f - K u)||^2
     double scale;   // 1/||r|| used to form the FP32 right-hand side
+    double rnorm;   // ||r||, the factor of the correction
     unsigned counter;
-    int pad;
+    float sigma;    // double-float residual: a power of two near 1/||D f||; FP32 sums of squares
+                    // run on sigma r, which keeps them clear of the FP32 range limits
 };
 
 struct SolveWs {
@@ -1078,12 +1119,13 @@ struct SolveWs {
     void *pcg;
     double *elem;  // 24 * n_elem corner contributions of the modal residual (FP64 or (h, l) float2)
     float2 *udd;   // double-float split of u (double-float residual)
+    float2 *fdd;   // and of D f
 };
 
 static size_t solve_ws_bytes_impl(int nx, int ny, int nz) {
     const size_t nd = (size_t)n_dof_of(nx, ny, nz);
     return 256 + al256(sizeof(OuterScalars)) + al256(nd * 8) + 2 * al256(nd * 4) + al256(3 * 4096 * 8) +
-           al256(pcg_ws_bytes_impl(nx, ny, nz)) + al256(apply_f64_modal_ws_bytes(nx, ny, nz)) + al256(nd * 8);
+           al256(pcg_ws_bytes_impl(nx, ny, nz)) + al256(apply_f64_modal_ws_bytes(nx, ny, nz)) + 2 * al256(nd * 8);
 }
 
 static SolveWs solve_ws(void *ws, int nx, int ny, int nz) {
@@ -1105,6 +1147,8 @@ static SolveWs solve_ws(void *ws, int nx, int ny, int nz) {
     w.elem = (double *)p;
     p += al256(apply_f64_modal_ws_bytes(nx, ny, nz));
     w.udd = (float2 *)p;
+    p += al256(nd * 8);
+    w.fdd = (float2 *)p;
     return w;
 }
 
@@ -1132,6 +1176,7 @@ __global__ void resid64_kernel(int64_t nd, const double *__restrict__ f, const d
     if (last_block3(rr, ff, 0.0, partials, &os->counter, tot) && threadIdx.x == 0) {
         os->rr = tot[0];
         os->ff = tot[1];
+        os->rnorm = sqrt(tot[0]);
         os->scale = tot[0] > 0.0 ? 1.0 / sqrt(tot[0]) : 0.0;
     }
 }
@@ -1139,14 +1184,37 @@ __global__ void resid64_kernel(int64_t nd, const double *__restrict__ f, const d
 // The node pass of the double-float residual: q_n = the (up to) 8 corner contributions of the
 // element pass summed in the fixed order b = 0..7 (double-float), then r = D(f - q) in FP64
 // and ||r||^2, ||D f||^2 -> os.
+// Once per solve, before the first double-float residual: fdd = the split of D f, and
+// ||D f||^2 (FP64, from f itself) with sigma = 2^-round(log2 ||D f||).
+__global__ void split_f_kernel(int64_t nd, const double *__restrict__ f, const uint8_t *__restrict__ mask, float2 *fdd,
+                               double *partials, OuterScalars *os) {
+    double ff = 0.0;
+    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
+        const bool fx = dof_fixed(mask, d);
+        const double v = fx ? 0.0 : f[d];
+        const ddv s = fx ? ddv{0.0f, 0.0f} : dd_split(v);
+        fdd[d] = make_float2(s.h, s.l);
+        ff = fma(v, v, ff);
+    }
+    __shared__ double tot[3];
+    if (last_block3(ff, 0.0, 0.0, partials, &os->counter, tot) && threadIdx.x == 0) {
+        os->ff = tot[0];
+        int e = 0;
+        if (tot[0] > 0.0 && isfinite(tot[0])) frexp(sqrt(tot[0]), &e);
+        e = e < -120 ? -120 : (e > 120 ? 120 : e);
+        os->sigma = ldexpf(1.0f, -e);
+    }
+}
+
 __global__ void __launch_bounds__(256) resid_dd_kernel(int nx, int ny, int nz, const FastDiv fNY, const FastDiv fNZ,
                                                        const float2 *__restrict__ C,
-                                                       const uint8_t *__restrict__ mask, const double *__restrict__ f,
-                                                       double *r, double *partials, OuterScalars *os) {
+                                                       const uint8_t *__restrict__ mask, const float2 *__restrict__ fdd,
+                                                       float2 *r, double *partials, OuterScalars *os) {
     const int64_t NY = ny + 1, NZ = nz + 1;
     const int64_t n_nodes = (int64_t)(nx + 1) * NY * NZ;
     const int64_t n_elem = (int64_t)nx * ny * nz;
-    double rr = 0.0, ff = 0.0;
+    const float sigma = os->sigma;
+    float rr = 0.0f;
     for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
         int i, j, k;
         unflatten3((uint32_t)n, fNY, fNZ, i, j, k);
@@ -1166,30 +1234,42 @@ __global__ void __launch_bounds__(256) resid_dd_kernel(int nx, int ny, int nz, c
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const bool fx = (m >> c) & 1;
-            const double fd = fx ? 0.0 : f[3 * n + c];
-            const double rd = fx ? 0.0 : fd - dd_value(acc[c]);
-            r[3 * n + c] = rd;
-            rr = fma(rd, rd, rr);
-            ff = fma(fd, fd, ff);
+            const float2 fv = fdd[3 * n + c];
+            const ddv rd = fx ? ddv{0.0f, 0.0f} : dd_add(ddv{fv.x, fv.y}, ddv{-acc[c].h, -acc[c].l});
+            r[3 * n + c] = make_float2(rd.h, rd.l);
+            // both parts: near convergence f and q agree in their leading parts and r lives in l
+            const float rs = __fmul_rn(__fadd_rn(rd.h, rd.l), sigma);
+            rr = fmaf(rs, rs, rr);
         }
     }
     __shared__ double tot[3];
-    if (last_block3(rr, ff, 0.0, partials, &os->counter, tot) && threadIdx.x == 0) {
-        os->rr = tot[0];
-        os->ff = tot[1];
-        os->scale = tot[0] > 0.0 ? 1.0 / sqrt(tot[0]) : 0.0;
+    if (last_block3_df(rr, 0.0f, 0.0f, (float2 *)partials, &os->counter, tot) && threadIdx.x == 0) {
+        const double s2 = (double)sigma * (double)sigma;
+        os->rr = tot[0] / s2;
+        os->rnorm = sqrt(tot[0]) / (double)sigma;
+        os->scale = tot[0] > 0.0 ? (double)sigma / sqrt(tot[0]) : 0.0;
     }
 }
 
-// u += d / scale (FP64), fixed DOFs zero, and its double-float split for the next residual.
+// b = r / ||r|| in FP32 from the double-float residual.
+__global__ void scale_dd_kernel(int64_t nd, const float2 *__restrict__ r, const OuterScalars *os, float *b) {
+    const float s = (float)os->scale;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 v = r[i];
+        b[i] = fmaf(v.x, s, v.y * s);
+    }
+}
+
+// u += ||r|| d (one FP64 fma), fixed DOFs zero, and its double-float split for the next
+// residual (integer conversions: f2d, dd_split).
 __global__ void correct_dd_kernel(int64_t nd, const float *__restrict__ d, const OuterScalars *os,
                                   const uint8_t *__restrict__ mask, double *u, float2 *udd) {
-    const double s = os->scale > 0.0 ? 1.0 / os->scale : 0.0;
+    const double s = os->rnorm;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x) {
         const bool fx = dof_fixed(mask, i);
-        const double v = fx ? 0.0 : fma((double)d[i], s, u[i]);
+        const double v = fx ? 0.0 : fma(f2d(d[i]), s, u[i]);
         u[i] = v;
-        const ddv w = fx ? ddv{0.0f, 0.0f} : dd_of(v);
+        const ddv w = fx ? ddv{0.0f, 0.0f} : dd_split(v);
         udd[i] = make_float2(w.h, w.l);
     }
 }
@@ -1205,7 +1285,7 @@ __global__ void scale_to_f32_kernel(int64_t nd, const double *__restrict__ r, co
 
 __global__ void correct64_kernel(int64_t nd, const float *__restrict__ d, const OuterScalars *os,
                                  const uint8_t *__restrict__ mask, double *u) {
-    const double s = os->scale > 0.0 ? 1.0 / os->scale : 0.0;
+    const double s = os->rnorm;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x)
         u[i] = dof_fixed(mask, i) ? 0.0 : fma((double)d[i], s, u[i]);
 }
@@ -1221,8 +1301,8 @@ static int outer_residual(const gbsimp_ctx *ctx, int nx, int ny, int nz, const g
         rc = elem_dd_modal(ctx, nx, ny, nz, law, x, w.udd, (float2 *)w.elem, st);
         if (rc) return rc;
         resid_dd_kernel<<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, fast_div(ny + 1), fast_div(nz + 1),
-                                                                  (const float2 *)w.elem, mask, f, w.r64,
-                                                                  w.partials, w.os);
+                                                                  (const float2 *)w.elem, mask, w.fdd,
+                                                                  (float2 *)w.r64, w.partials, w.os);
         GBS_LAUNCH_CHECK("resid_dd_kernel");
         return GBS_OK;
     }
@@ -1244,6 +1324,30 @@ static int outer_correct(const gbsimp_ctx *ctx, int64_t nd, const uint8_t *mask,
     } else {
         correct64_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.d32, w.os, mask, u);
         GBS_LAUNCH_CHECK("correct64_kernel");
+    }
+    return GBS_OK;
+}
+
+// Before the first residual of a solve: the double-float splits of u and D f, ||D f||^2.
+static int outer_start(const gbsimp_ctx *ctx, int64_t nd, const double *u, const double *f, const uint8_t *mask,
+                       bool dd, const SolveWs &w, cudaStream_t st) {
+    if (!dd) return GBS_OK;
+    int rc = split_dd(ctx, nd, u, mask, w.udd, st);
+    if (rc) return rc;
+    split_f_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, f, mask, w.fdd, w.partials, w.os);
+    GBS_LAUNCH_CHECK("split_f_kernel");
+    return GBS_OK;
+}
+
+// The FP32 right-hand side b32 = r / ||r|| of the next inner solve (its x0 = 0 is written by
+// the PCG setup).
+static int outer_scale(const gbsimp_ctx *ctx, int64_t nd, bool dd, const SolveWs &w, cudaStream_t st) {
+    if (dd) {
+        scale_dd_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, (const float2 *)w.r64, w.os, w.b32);
+        GBS_LAUNCH_CHECK("scale_dd_kernel");
+    } else {
+        scale_to_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.r64, w.os, w.b32, w.d32);
+        GBS_LAUNCH_CHECK("scale_to_f32_kernel");
     }
     return GBS_OK;
 }
@@ -1282,8 +1386,8 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
     const PcgScalars *pending = nullptr;
     const PcgWs pw = pcg_ws(w.pcg, nx, ny, nz);
     const bool dd = use_dd_residual(ctx, o);
-    if (dd) {
-        int rc = split_dd(ctx, nd, u, mask, w.udd, st);
+    {
+        int rc = outer_start(ctx, nd, u, f, mask, dd, w, st);
         if (rc) return rc;
     }
     for (;;) {
@@ -1319,8 +1423,8 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
             status = GBS_ENOTCONV;
             break;
         }
-        scale_to_f32_kernel<<<vb, 256, 0, st>>>(nd, w.r64, w.os, w.b32, w.d32);
-        GBS_LAUNCH_CHECK("scale_to_f32_kernel");
+        rc = outer_scale(ctx, nd, dd, w, st);
+        if (rc) return rc;
         // Inner tolerance: enough to reach rtol from here, but not below what FP32 resolves.
         double itol = o->rtol / relres;
         if (itol < inner) itol = inner;
@@ -1753,10 +1857,8 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
             SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
             if (it.stats.outer == 0) {
                 GBS_CUDA_TRY(cudaMemsetAsync(w.os, 0, sizeof(OuterScalars), st));
-                if (dd) {
-                    int rc = split_dd(ctx, n_dof_of(it.nx, it.ny, it.nz), it.u, it.node_mask, w.udd, st);
-                    if (rc) return rc;
-                }
+                int rc = outer_start(ctx, n_dof_of(it.nx, it.ny, it.nz), it.u, it.f, it.node_mask, dd, w, st);
+                if (rc) return rc;
             }
             int rc = outer_residual(ctx, it.nx, it.ny, it.nz, glaw, it.x, it.f, it.node_mask, it.u, dd, w, st);
             if (rc) return rc;
@@ -1797,8 +1899,8 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
         gbsimp_batch_item &it = items[i];
         const int64_t nd = n_dof_of(it.nx, it.ny, it.nz);
         SolveWs w = solve_ws(it.ws, it.nx, it.ny, it.nz);
-        scale_to_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.r64, w.os, w.b32, w.d32);
-        GBS_LAUNCH_CHECK("scale_to_f32_kernel");
+        int src = outer_scale(ctx, nd, dd, w, st);
+        if (src) return src;
         double itol = o->rtol / it.stats.relres;
         if (itol < inner) itol = inner;
         PcgWs pw = pcg_ws(w.pcg, it.nx, it.ny, it.nz);

@@ -11,9 +11,16 @@ from genpipeline_gb300.serve import FEMServer, request_stream
 
 pytestmark = pytest.mark.gpu
 
-# Every design is solved to ||D(f - K u)|| <= 1e-8 ||D f|| (FP64 residual) on both paths, so
-# displacements agree to ~1e-6 of their maximum and compliances to ~1e-7 relative.
-U_TOL, C_TOL = 1e-6, 1e-7
+# Every design is solved to ||D(f - K u)|| <= 1e-8 ||D f|| on both paths, so displacements
+# agree to ~1e-6 of their maximum. Two such solutions u1, u2 have compliances that differ by
+# f.(u1 - u2) = u.(r2 - r1) (K symmetric), at most 2e-8 ||u|| ||D f||: the tests allow twice that.
+U_TOL, RELRES = 1e-6, 1e-8
+
+
+def _c_bound(u, f, fixed):
+    fd = np.asarray(f, dtype=np.float64).copy()
+    fd[np.asarray(fixed, dtype=np.int64)] = 0.0
+    return 4 * RELRES * float(np.linalg.norm(u)) * float(np.linalg.norm(fd))
 
 
 def _designs():
@@ -49,7 +56,7 @@ def test_batch_equals_single_solves(fused, round_iters, share, group):
         assert b.stats["status"] == L.GBS_OK and b.stats["relres"] <= 1e-8, b.stats
         us, ub = s.du.cpu().numpy(), b.du.cpu().numpy()
         np.testing.assert_allclose(ub, us, rtol=0, atol=U_TOL * np.abs(us).max())
-        assert b.compliance == pytest.approx(s.compliance, rel=C_TOL)
+        assert abs(b.compliance - s.compliance) <= _c_bound(us, s.f, s.fixed_dofs)
 
 
 def test_autotuned_batch_equals_single_solves(tmp_path):
@@ -70,7 +77,7 @@ def test_autotuned_batch_equals_single_solves(tmp_path):
     for d in single:
         b = by_grid[d.grid]
         assert b.stats["status"] == L.GBS_OK and b.stats["relres"] <= 1e-8, b.stats
-        assert b.compliance == pytest.approx(d.compliance, rel=C_TOL)
+        assert abs(b.compliance - d.compliance) <= _c_bound(d.du.cpu().numpy(), d.f, d.fixed_dofs)
 
 
 def test_serving_results_equal_alone_and_in_the_mix():
@@ -85,8 +92,8 @@ def test_serving_results_equal_alone_and_in_the_mix():
         grid = (r.n, r.n, r.n)
         f, fixed = D.load_case(r.load, r.n)
         alone = solve_plain([FEMDesign(grid, D.grf_density(grid, r.seed), f, fixed)], eng)[0]
-        assert r.compliance == pytest.approx(alone.compliance, rel=C_TOL), r
         ua = alone.du.cpu().numpy()
+        assert abs(r.compliance - alone.compliance) <= _c_bound(ua, f, fixed), r
         np.testing.assert_allclose(r.u.cpu().numpy(), ua, rtol=0, atol=U_TOL * np.abs(ua).max())
     warm = [r for r in reqs if r.warm]
     cold = {(r.n, r.seed, r.load): r.iterations for r in reqs if not r.warm}

@@ -84,5 +84,8 @@ def test_queue_matches_one_solve_per_design():
         assert d.stats["status"] == L.GBS_OK and d.stats["relres"] <= 1e-8, d.stats
         up, uq = p.du.cpu().numpy(), d.du.cpu().numpy()
         np.testing.assert_allclose(uq, up, rtol=0, atol=1e-6 * np.abs(up).max())
-        assert d.compliance == pytest.approx(p.compliance, rel=1e-7)
+        # both solves certify ||D(f - K u)|| <= 1e-8 ||D f||: f.(u1 - u2) = u.(r2 - r1) <= 2e-8 ||u|| ||D f||
+        fd = np.asarray(p.f, dtype=np.float64).copy()
+        fd[np.asarray(p.fixed_dofs, dtype=np.int64)] = 0.0
+        assert abs(d.compliance - p.compliance) <= 4e-8 * np.linalg.norm(up) * np.linalg.norm(fd)
     q.close()
