@@ -161,8 +161,8 @@ __global__ void __launch_bounds__(128) modal_elem_dd_kernel(int nx, int ny, int 
 }
 
 int split_dd(const gbsimp_ctx *ctx, int64_t nd, const double *u, const uint8_t *mask, float2 *udd, cudaStream_t st) {
-    int64_t b = (nd + 255) / 256;
-    const int64_t cap = 4LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+    int64_t b = (nd + 255) / 256;  // about one DOF per thread (elementwise)
+    const int64_t cap = 64LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
     split_dd_kernel<<<(unsigned)(b < cap ? (b < 1 ? 1 : b) : cap), 256, 0, st>>>(nd, u, mask, udd);
     GBS_LAUNCH_CHECK("split_dd_kernel");
     return GBS_OK;

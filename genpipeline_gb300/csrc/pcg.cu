@@ -34,9 +34,19 @@ static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 static inline int64_t n_dof_of(int nx, int ny, int nz) { return 3LL * (nx + 1) * (ny + 1) * (nz + 1); }
 
+// Blocks of 256 threads for a vector kernel that ends in a last-block reduction (at most 8 per
+// SM: the partials hold 4096 per sum, and the last block sums them all).
 static inline unsigned vec_blocks(const gbsimp_ctx *ctx, int64_t n) {
     int64_t b = (n + 255) / 256;
-    const int64_t cap = 4LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+    const int64_t cap = 8LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
+    if (b > cap) b = cap;
+    return (unsigned)(b < 1 ? 1 : b);
+}
+// ... and for an elementwise kernel: about one element per thread, so that the loads of every
+// element are in flight together rather than one grid-stride round trip after another.
+static inline unsigned ew_blocks(const gbsimp_ctx *ctx, int64_t n) {
+    int64_t b = (n + 255) / 256;
+    const int64_t cap = 64LL * (ctx->num_sms > 0 ? ctx->num_sms : 148);
     if (b > cap) b = cap;
     return (unsigned)(b < 1 ? 1 : b);
 }
@@ -190,11 +200,11 @@ __device__ bool last_block3(double a, double b, double c, double *partials, unsi
 // The same for FP32 per-thread partials, in double-float on the FP32 pipe (block sums, the
 // per-block partials and the last block's sum in block order); the totals in out[] are valid
 // in thread 0 of the last block.
-__device__ bool last_block3_df(float a, float b, float c, float2 *partials, unsigned *counter, double *out) {
+__device__ bool last_block3_df(df32 a, df32 b, df32 c, float2 *partials, unsigned *counter, double *out) {
     __shared__ float2 sred[3 * 32];
     __shared__ bool last;
     const int nblk = gridDim.x;
-    df32 v[3] = {{a, 0.0f}, {b, 0.0f}, {c, 0.0f}};
+    df32 v[3] = {a, b, c};
     block_sum_df<3>(v, sred);
     if (threadIdx.x == 0) {
 #pragma unroll
@@ -219,6 +229,10 @@ __device__ bool last_block3_df(float a, float b, float c, float2 *partials, unsi
         *counter = 0;
     }
     return true;
+}
+__device__ __forceinline__ bool last_block3_df(float a, float b, float c, float2 *partials, unsigned *counter,
+                                               double *out) {
+    return last_block3_df(df32{a, 0.0f}, df32{b, 0.0f}, df32{c, 0.0f}, partials, counter, out);
 }
 
 // r = D b - q (q = D K D x0), x0 fixed entries zeroed, p_{-1} = 0; sums r.z, r.r, (Db).(Db).
@@ -950,12 +964,12 @@ static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp
     }
     GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
     if (!(flags & SETUP_KEEP_DINV)) {
-        dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, fast_div(ny + 1), fast_div(nz + 1), law,
+        dinv_kernel<float><<<ew_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, fast_div(ny + 1), fast_div(nz + 1), law,
                                                                      ctx->kef, x, mask, w.dinv);
         GBS_LAUNCH_CHECK("dinv_kernel");
         if (use_modal(ctx, nz)) {
             const int64_t ne = (int64_t)nx * ny * nz;
-            moduli_f32_kernel<<<vec_blocks(ctx, ne), 256, 0, st>>>(ne, law, x, w.E);
+            moduli_f32_kernel<<<ew_blocks(ctx, ne), 256, 0, st>>>(ne, law, x, w.E);
             GBS_LAUNCH_CHECK("moduli_f32_kernel");
         }
     }
@@ -1024,7 +1038,7 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
     if (!prof && !h.done && fused) {
         const FusedItem item{nx, ny, nz, x, mask, u, w};
         if (pcg_fused_batch(ctx, &item, 1, law, st) == GBS_OK) {
-            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, 0);
+            pcg_finalize_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, 0);
             GBS_LAUNCH_CHECK("pcg_finalize_kernel");
             if (async) return GBS_OK;
             rc = read_scalars(w.sc, &h, st);
@@ -1041,7 +1055,7 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
             if (lrc) return lrc;  // the launch itself failed
             rc = cg_publish(ctx, nx, ny, nz, w, 1, st);
             if (rc) return rc;
-            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 2 : 1);
+            pcg_finalize_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 2 : 1);
             GBS_LAUNCH_CHECK("pcg_finalize_kernel");
             if (async) return GBS_OK;  // the caller counts the loop's launches from the scalars
             rc = read_scalars(w.sc, &h, st);
@@ -1092,7 +1106,7 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
         if (check_every <= 0 && chunk < max_chunk) chunk *= 2;
     }
     for (auto &e : ev) cudaEventDestroy(e);
-    pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 2 : 1);
+    pcg_finalize_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 2 : 1);
     GBS_LAUNCH_CHECK("pcg_finalize_kernel");
     rc = read_scalars(w.sc, &h, st);
     if (rc) return rc;
@@ -1197,7 +1211,9 @@ __global__ void split_f_kernel(int64_t nd, const double *__restrict__ f, const u
         ff = fma(v, v, ff);
     }
     __shared__ double tot[3];
-    if (last_block3(ff, 0.0, 0.0, partials, &os->counter, tot) && threadIdx.x == 0) {
+    const ddv fs = dd_split(ff);  // the thread's FP64 partial, summed on in double-float
+    if (last_block3_df(df32{fs.h, fs.l}, df32{0.0f, 0.0f}, df32{0.0f, 0.0f}, (float2 *)partials, &os->counter, tot) &&
+        threadIdx.x == 0) {
         os->ff = tot[0];
         int e = 0;
         if (tot[0] > 0.0 && isfinite(tot[0])) frexp(sqrt(tot[0]), &e);
@@ -1319,10 +1335,10 @@ static int outer_residual(const gbsimp_ctx *ctx, int nx, int ny, int nz, const g
 static int outer_correct(const gbsimp_ctx *ctx, int64_t nd, const uint8_t *mask, double *u, bool dd,
                          const SolveWs &w, cudaStream_t st) {
     if (dd) {
-        correct_dd_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.d32, w.os, mask, u, w.udd);
+        correct_dd_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, w.d32, w.os, mask, u, w.udd);
         GBS_LAUNCH_CHECK("correct_dd_kernel");
     } else {
-        correct64_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.d32, w.os, mask, u);
+        correct64_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, w.d32, w.os, mask, u);
         GBS_LAUNCH_CHECK("correct64_kernel");
     }
     return GBS_OK;
@@ -1343,10 +1359,10 @@ static int outer_start(const gbsimp_ctx *ctx, int64_t nd, const double *u, const
 // the PCG setup).
 static int outer_scale(const gbsimp_ctx *ctx, int64_t nd, bool dd, const SolveWs &w, cudaStream_t st) {
     if (dd) {
-        scale_dd_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, (const float2 *)w.r64, w.os, w.b32);
+        scale_dd_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, (const float2 *)w.r64, w.os, w.b32);
         GBS_LAUNCH_CHECK("scale_dd_kernel");
     } else {
-        scale_to_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, w.r64, w.os, w.b32, w.d32);
+        scale_to_f32_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, w.r64, w.os, w.b32, w.d32);
         GBS_LAUNCH_CHECK("scale_to_f32_kernel");
     }
     return GBS_OK;
@@ -1643,20 +1659,20 @@ extern "C" int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, co
         if (rc) return rc;
     }
     GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
-    dinv_kernel<float><<<vec_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, fast_div(ny + 1), fast_div(nz + 1), law,
+    dinv_kernel<float><<<ew_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, fast_div(ny + 1), fast_div(nz + 1), law,
                                                                  ctx->kef, x, node_mask, w.dinv);
-    fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 1.0f, w.r);
-    fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.p1);
-    fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, xu);
+    fill_f32_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, 1.0f, w.r);
+    fill_f32_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.p1);
+    fill_f32_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, xu);
     if (modal) {  // launches alternate the buffer parity: give both parities the same state
         const int64_t ne = (int64_t)nx * ny * nz;
-        moduli_f32_kernel<<<vec_blocks(ctx, ne), 256, 0, st>>>(ne, law, x, w.E);
-        fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 1.0f, w.r1);
-        fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.ap);
-        fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.s0);
-        fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.s1);
-        fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.p0);
-        fill_f32_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.w2);
+        moduli_f32_kernel<<<ew_blocks(ctx, ne), 256, 0, st>>>(ne, law, x, w.E);
+        fill_f32_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, 1.0f, w.r1);
+        fill_f32_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.ap);
+        fill_f32_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.s0);
+        fill_f32_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.s1);
+        fill_f32_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.p0);
+        fill_f32_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, 0.0f, w.w2);
         freeze_scalars_kernel<<<1, 1, 0, st>>>(w.sc);
     }
     GBS_LAUNCH_CHECK("time_pcg_apply setup");
@@ -1999,7 +2015,7 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
             PcgWs pw = pcg_ws(w.pcg, it.nx, it.ny, it.nz);
             // one-kernel graph loop: x may owe a half step; persistent: complete
             const bool graph_loop = k + j >= n_fused;
-            pcg_finalize_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, pw.p0, pw.p1, w.d32, pw.sc,
+            pcg_finalize_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, pw.p0, pw.p1, w.d32, pw.sc,
                                                                     use_modal(ctx, it.nz) ? (graph_loop ? 2 : 0) : 1);
             GBS_LAUNCH_CHECK("pcg_finalize_kernel");
             GBS_CUDA_TRY(cudaMemcpyAsync((char *)hp + j * ps, pw.sc, ps, cudaMemcpyDeviceToHost, st));
