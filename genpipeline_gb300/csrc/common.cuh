@@ -274,10 +274,14 @@ __device__ __forceinline__ ddv dd_of(double v) {
 __device__ __forceinline__ double dd_value(ddv a) { return (double)a.h + (double)a.l; }
 // (double)x from the bits of a normal FP32 x (exponent rebiased, mantissa widened); zero,
 // subnormals, infinities and NaN take the conversion instruction.
+// The rare paths below are calls, so that the compiler branches around their conversion
+// instructions instead of predicating them into every evaluation.
+static __device__ __noinline__ double f2d_slow(float x) { return (double)x; }
 __device__ __forceinline__ double f2d(float x) {
     const unsigned b = __float_as_uint(x);
     const unsigned e = (b >> 23) & 0xffu;
-    if (e == 0u || e == 0xffu) return (b & 0x7fffffffu) == 0u ? (b ? -0.0 : 0.0) : (double)x;
+    if ((b & 0x7fffffffu) == 0u) return __longlong_as_double((long long)((unsigned long long)(b >> 31) << 63));
+    if (e == 0u || e == 0xffu) return f2d_slow(x);
     return __longlong_as_double((long long)(((unsigned long long)(b >> 31) << 63) |
                                             ((unsigned long long)(e + 896u) << 52) |
                                             ((unsigned long long)(b & 0x7fffffu) << 29)));
@@ -288,10 +292,12 @@ __device__ __forceinline__ double f2d(float x) {
 // difference of the patterns counts mantissa units across a binade carry too), rounded to
 // FP32 by the integer conversion and scaled exactly. Values with |v| outside [2^-70, 2^100],
 // and zero, subnormals, infinities and NaN, take dd_of.
+static __device__ __noinline__ ddv dd_of_slow(double v) { return dd_of(v); }
 __device__ __forceinline__ ddv dd_split(double v) {
     const long long b = __double_as_longlong(v);
     const int e = (int)((b >> 52) & 0x7ff);
-    if (e < 1023 - 70 || e > 1023 + 100) return dd_of(v);
+    if ((b & 0x7fffffffffffffffLL) == 0) return ddv{0.0f, 0.0f};
+    if (e < 1023 - 70 || e > 1023 + 100) return dd_of_slow(v);
     const long long rb = (b + ((1LL << 28) - 1) + ((b >> 29) & 1)) & ~((1LL << 29) - 1);
     const int eh = (int)((rb >> 52) & 0x7ff);
     const unsigned sign = (unsigned)((unsigned long long)b >> 63) << 31;
