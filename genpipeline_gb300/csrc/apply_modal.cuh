@@ -93,6 +93,11 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsign
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
 }
+// A bulk prefetch of a global range into L2 (sm_90+; 16-byte aligned, a multiple of 16 bytes):
+// no shared memory and no completion to wait for.
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, unsigned bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
     unsigned ok;
     asm volatile(
@@ -348,22 +353,47 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
         bphase ^= 1u;
     };
     const int64_t full = NW & ~(int64_t)3;  // words of the vectors in whole 16-byte groups
+    // Whole 16-byte groups of node plane j: [g0, g0 + nfull) of the plane-wide vectors and
+    // [o0, o0 + nown) of the owned ones (p, x).
+    auto plane_ranges = [&](int j, int64_t &g0, unsigned &nfull, int64_t &o0, unsigned &nown) {
+        const PlaneW P = plane_w(j);
+        nfull = 0;
+        nown = 0;
+        g0 = 0;
+        o0 = 0;
+        if (P.pv) {
+            g0 = max(P.A, (int64_t)0);
+            const int64_t g1 = min(P.A + 4 * (int64_t)P.nv, full);
+            if (g1 > g0) nfull = (unsigned)(g1 - g0);
+            if (CG && P.own) {  // groups that meet the owned words [olo3, ohi3)
+                o0 = max(P.A + 4 * (int64_t)((P.olo3 + P.pad) >> 2), (int64_t)0);
+                const int64_t o1 = min(P.A + 4 * (int64_t)((P.ohi3 + P.pad + 3) >> 2), full);
+                if (o1 > o0) nown = (unsigned)(o1 - o0);
+            }
+        }
+    };
+    // L2 prefetch of node plane j (the plane after the one whose copies are in flight): its
+    // DRAM reads start a step earlier than its copies into shared memory, with no shared memory
+    // held for them.
+    auto prefetch_plane = [&](int j) {
+        int64_t g0, o0;
+        unsigned nfull, nown;
+        plane_ranges(j, g0, nfull, o0, nown);
+        if (nfull)
+#pragma unroll
+            for (int a = 0; a < NF; ++a) bulk_prefetch_l2(src_of(a) + g0, 4u * nfull);
+        if (CG && nown)
+#pragma unroll
+            for (int a = 4; a < 6; ++a)
+                if (a == 4 || cp.xmode) bulk_prefetch_l2(src_of(a) + o0, 4u * nown);
+    };
     auto issue_plane = [&](int j) {
         {
             if (tid == 0) {
                 const PlaneW P = plane_w(j);
-                unsigned nfull = 0, nown = 0;
-                int64_t g0 = 0, o0 = 0;
-                if (P.pv) {
-                    g0 = max(P.A, (int64_t)0);
-                    const int64_t g1 = min(P.A + 4 * (int64_t)P.nv, full);
-                    if (g1 > g0) nfull = (unsigned)(g1 - g0);
-                    if (CG && P.own) {  // groups that meet the owned words [olo3, ohi3)
-                        o0 = max(P.A + 4 * (int64_t)((P.olo3 + P.pad) >> 2), (int64_t)0);
-                        const int64_t o1 = min(P.A + 4 * (int64_t)((P.ohi3 + P.pad + 3) >> 2), full);
-                        if (o1 > o0) nown = (unsigned)(o1 - o0);
-                    }
-                }
+                int64_t g0, o0;
+                unsigned nfull, nown;
+                plane_ranges(j, g0, nfull, o0, nown);
                 const unsigned nown_vec = cp.xmode ? 2u : 1u;  // p, and x when it is updated
                 mbar_arrive_expect_tx(&s_bar, 4u * (NF * nfull + nown_vec * nown));
                 fence_proxy_async();
@@ -376,6 +406,8 @@ __device__ __forceinline__ bool modal_pass(const ModalGeom &G, const float *__re
                     for (int a = 4; a < 6; ++a)
                         if (a == 4 || cp.xmode)
                             bulk_copy_g2s(Raw + a * RW + (o0 - P.A), src_of(a) + o0, 4u * nown, &s_bar);
+                // the PCG modes (several vectors per plane): the plain apply measured no gain
+                if (CG && j + 1 <= xe) prefetch_plane(j + 1);  // xe: the segment's last staged plane
             }
             // the group cut by the end of the vectors: only the last node plane reaches it
             if (j == nx && full < NW) {
