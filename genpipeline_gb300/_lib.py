@@ -131,6 +131,7 @@ SIGNATURES = {
     "gbsimp_pcg_csr_f32": (_I, [_P, _I64, _P, _P, _P, _P, _P, _P, _P, _I64, C.POINTER(SolveOpts),
                                 C.POINTER(SolveStats), _P, _SZ, _P]),
     "gbsimp_dot_f64": (_I, [_P, _I64, _P, _P, _P, _P, _SZ, _P]),
+    "gbsimp_warm_start": (_I, [_P, _I64, _P, _P, _D, _P]),
     "gbsimp_voxel_prep_ws_bytes": (_SZ, [_I, _I, _I, _I, _I, _I, _I]),
     "gbsimp_voxel_prep": (_I, [_P, _I, _I, _I, _I, _P, _I, _I, _I, _P, _D, _D, _P, _SZ, _P]),
     "gbsimp_barrier_selftest_ws_bytes": (_SZ, []),

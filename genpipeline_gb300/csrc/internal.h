@@ -37,6 +37,8 @@ int apply_f64_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_
 int split_dd(const gbsimp_ctx *ctx, int64_t nd, const double *u, const uint8_t *mask, float2 *udd, cudaStream_t st);
 int elem_dd_modal(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
                   const float2 *udd, float2 *C, cudaStream_t st);
+// gbsimp_warm_start without the argument checks (the native SIMP loop).
+int warm_start_impl(const gbsimp_ctx *ctx, int64_t n, double *u, double *u_prev, double theta, cudaStream_t st);
 // OC update with an explicit scratch pointer (layout of gbsimp_oc_ws_bytes).
 size_t oc_ws_bytes_impl(int64_t n_elem);
 // The filter row sums Hs inside an OC workspace (valid after oc_prepare_impl).

@@ -1473,6 +1473,22 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
     return GBS_OK;
 }
 
+// ---- warm start of a SIMP loop's next solve ---------------------------------------------------
+__global__ void warm_start_kernel(int64_t n, double *__restrict__ u, double *__restrict__ up, double theta) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double t = u[i];
+        u[i] = fma(theta, t - up[i], t);
+        up[i] = t;
+    }
+}
+
+int warm_start_impl(const gbsimp_ctx *ctx, int64_t n, double *u, double *u_prev, double theta, cudaStream_t st) {
+    if (n <= 0) return GBS_OK;
+    warm_start_kernel<<<ew_blocks(ctx, n), 256, 0, st>>>(n, u, u_prev, theta);
+    GBS_LAUNCH_CHECK("warm_start_kernel");
+    return GBS_OK;
+}
+
 // ---- CSR Jacobi-PCG (pcg_solve_cuda contract) -------------------------------------------------
 struct CsrScalars {
     double rz, rr, bnorm, alpha, beta, pap;
@@ -1761,6 +1777,13 @@ extern "C" int gbsimp_pcg_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbs
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     return GBS_OK;
+}
+
+extern "C" int gbsimp_warm_start(gbsimp_ctx *ctx, int64_t n, double *u, double *u_prev, double theta,
+                                 void *stream) {
+    if (!ctx || n < 0 || (n > 0 && (!u || !u_prev)) || !isfinite(theta))
+        return set_error(GBS_EINVAL, "gbsimp_warm_start: bad arguments");
+    return warm_start_impl(ctx, n, u, u_prev, theta, (cudaStream_t)stream);
 }
 
 extern "C" int gbsimp_solve(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,

@@ -18,17 +18,22 @@ constexpr size_t kAlign = 256;
 size_t al(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
 
 // Workspace: [solve ws][OC ws (holds Hs)][sensitivity ws][dc][dcf][xnew][objective (double)]
+// [the previous solution (FP64), for the extrapolated warm start]
 struct SimpWs {
     void *solve, *oc, *sens;
     size_t solve_bytes, oc_bytes, sens_bytes;
     float *dc, *dcf, *xnew;
-    double *obj;
+    double *obj, *u_prev;
 };
+
+// Warm start of solve k >= 3: u_{k-1} + theta (u_{k-1} - u_{k-2}) (gbsimp_warm_start).
+constexpr double kWarmTheta = 0.5;
 
 size_t simp_ws_bytes(int nx, int ny, int nz) {
     const size_t ne = (size_t)nx * ny * nz;
     return kAlign + al(gbsimp_solve_ws_bytes(nx, ny, nz)) + al(oc_ws_bytes_impl((int64_t)ne)) +
-           al(gbsimp_sensitivity_ws_bytes(nx, ny, nz)) + 3 * al(ne * sizeof(float)) + al(sizeof(double));
+           al(gbsimp_sensitivity_ws_bytes(nx, ny, nz)) + 3 * al(ne * sizeof(float)) + al(sizeof(double)) +
+           al(3 * (size_t)(nx + 1) * (ny + 1) * (nz + 1) * sizeof(double));
 }
 
 SimpWs simp_ws(void *ws, int nx, int ny, int nz) {
@@ -51,6 +56,8 @@ SimpWs simp_ws(void *ws, int nx, int ny, int nz) {
     w.xnew = (float *)p;
     p += al(ne * sizeof(float));
     w.obj = (double *)p;
+    p += al(sizeof(double));
+    w.u_prev = (double *)p;
     return w;
 }
 
@@ -92,7 +99,17 @@ extern "C" int gbsimp_simp_run(gbsimp_ctx *ctx, int nx, int ny, int nz, const gb
     double prev = 0.0;
     int below = 0, it = 0;
     gbsimp_solve_stats sstats = {};
+    const int64_t nd = 3LL * (nx + 1) * (ny + 1) * (nz + 1);
     for (; it < opts->n_iters; ++it) {
+        // u holds the last solution from the second iteration on, u_prev the one before from the
+        // third on (the caller's initial u is not a solution of this loop)
+        if (it >= 2) {
+            rc = warm_start_impl(ctx, nd, u, w.u_prev, kWarmTheta, st);
+        } else if (it == 1) {
+            const cudaError_t e = cudaMemcpyAsync(w.u_prev, u, (size_t)nd * sizeof(double), cudaMemcpyDeviceToDevice, st);
+            rc = e == cudaSuccess ? GBS_OK : cuda_error(e, "cudaMemcpyAsync(u_prev)");
+        }
+        if (rc) break;
         rc = gbsimp_solve(ctx, nx, ny, nz, law, xphys, f, node_mask, u, &opts->solve, &sstats, w.solve,
                           w.solve_bytes, stream);
         if (rc) break;

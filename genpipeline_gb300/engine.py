@@ -345,6 +345,12 @@ class Engine:
                                                    _p(out), out.shape[0], C.byref(m), _p(ws), nb, _stream()))
         return out
 
+    def warm_start(self, u: torch.Tensor, u_prev: torch.Tensor, theta: float) -> None:
+        """u <- u + theta (u - u_prev), u_prev <- old u (gbsimp_warm_start), in place."""
+        _need(u, torch.float64, u.numel(), "u")
+        _need(u_prev, torch.float64, u.numel(), "u_prev")
+        L.check(self.lib.gbsimp_warm_start(self.ctx, u.numel(), _p(u), _p(u_prev), float(theta), _stream()))
+
     def dot64(self, a: torch.Tensor, b: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         _need(a, torch.float64, a.numel(), "a")
         _need(b, torch.float64, a.numel(), "b")

@@ -39,6 +39,9 @@ class SolveSpec:
     max_iter: int = 200000
     max_outer: int = 30
     fused: bool = False         # persistent one-launch PCG (grid barriers) instead of the graph loop
+    # warm start of solve k >= 3: u_{k-1} + warm_theta (u_{k-1} - u_{k-2}) (0: u_{k-1}); the value
+    # of the native loop (gbsimp_simp_run), whose designs this loop reproduces bit for bit
+    warm_theta: float = 0.5
 
     def material(self) -> L.Law:
         return L.make_law(self.law, self.penal, self.e0, self.emin, self.xmin)
@@ -77,6 +80,8 @@ class SimpProblem:
             self.x[self.pres.bool()] = 1.0
         self.xphys = self.x.clone()
         self.u = torch.zeros(nd, dtype=torch.float64, device=dev)
+        self.u_prev = torch.zeros(nd, dtype=torch.float64, device=dev)
+        self.solved = 0  # solutions of this loop held in u (and u_prev)
         self.dc = torch.empty(ne, dtype=torch.float32, device=dev)
         self.dcf = torch.empty(ne, dtype=torch.float32, device=dev)
         self.xnew = torch.empty(ne, dtype=torch.float32, device=dev)
@@ -101,7 +106,12 @@ class SimpProblem:
     def step(self) -> dict:
         """One OC iteration of the reference loop."""
         s = self.spec
+        if s.warm_theta > 0.0 and self.solved >= 2:
+            self.eng.warm_start(self.u, self.u_prev, s.warm_theta)
+        elif self.solved == 1:
+            self.u_prev.copy_(self.u)
         st = self.solve()
+        self.solved += 1
         self.eng.sensitivity(self.grid, self.law, self.xphys, self.u, dc=self.dc, energy=self.energy)
         self.eng.filter(self.grid, s.rmin, self.dc, hs=self.hs, transpose=True, out=self.dcf)
         self.eng.oc(self.grid, s.rmin, s.volfrac, self.x, self.dcf, self.pres, s.oc_variant, xnew=self.xnew,
@@ -110,6 +120,18 @@ class SimpProblem:
         self.iteration += 1
         self.history.append(st)
         return st
+
+    def state(self):
+        """A copy of the loop's state (design, xPhys, displacements and the warm-start history)."""
+        return (self.x.clone(), self.xphys.clone(), self.u.clone(), self.u_prev.clone(), self.solved)
+
+    def restore(self, state) -> None:
+        x, xphys, u, u_prev, solved = state
+        self.x.copy_(x)
+        self.xphys.copy_(xphys)
+        self.u.copy_(u)
+        self.u_prev.copy_(u_prev)
+        self.solved = solved
 
     def compliance(self) -> float:
         """f . u of the current displacement (synchronises)."""

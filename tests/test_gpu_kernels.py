@@ -432,3 +432,12 @@ def test_library_rejects_bad_arguments(eng):
         eng.filter((4, 4, 4), 7.5, torch.zeros(64, device="cuda"))
     with pytest.raises(L.GbsimpError):
         L.check(eng.lib.gbsimp_apply_f32(eng.ctx, 0, 1, 1, lw, None, None, None, None, None))
+
+
+def test_warm_start_extrapolation(eng):
+    rng = np.random.default_rng(4)
+    a, b = rng.standard_normal(1000), rng.standard_normal(1000)
+    u, up = _cuda(a), _cuda(b)
+    eng.warm_start(u, up, 0.5)
+    np.testing.assert_allclose(u.cpu().numpy(), a + 0.5 * (a - b), rtol=1e-15, atol=1e-15)
+    assert np.array_equal(up.cpu().numpy(), a)
