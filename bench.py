@@ -656,7 +656,7 @@ def run_serve(a):
     line = {"metric": METRIC, "value": summ["solves_per_s"], "unit": "FEM solves/s", "n_gpus": 1,
             "steps": summ["requests"], "warmup": 40, "ms_per_step": 1e3 / summ["solves_per_s"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 (FP64 outer residual, dots, compliance)", "data": "synthetic", "impl": "ours",
+            "dtype": "f32 (outer residual in double-float FP32 pairs with FP64 u; compensated FP32 dots; FP64 compliance)", "data": "synthetic", "impl": "ours",
             "config": {"workload": "fem_serving_stream", "requests": summ["requests"], "rate_per_s": 200.0,
                        "edges": [24, 32, 48, 64, 96], "loads": ["cantilever", "top_patch", "torsion"],
                        "repeat_fraction": 0.1, "rtol": 1e-8, "max_slots": 24, "round_iters": SERVE_ROUND_ITERS,
@@ -752,6 +752,29 @@ def run_ours(a):
     e2e = {"value": whole_job_rate(world, a.steps, te), "unit": UNIT, "h2d_bytes_per_step": 4 * ne,
            "d2h_bytes_per_step": 8 * ne}
 
+    # ---- the same timed steps with the outer residual's element products in FP64 ----------
+    # (the default forms them in double-float FP32 pairs, FP64 u and norms; GB300's FP64 pipe
+    # makes the FP64 form the slower one)
+    state_after = prob.state()
+    prob.restore(snap)
+    prob.spec.residual_fp64 = True
+    barrier()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record()
+    its64 = 0
+    for _ in range(a.steps):
+        flush.zero_()
+        its64 += prob.step()["iterations"]
+    f1.record()
+    barrier()
+    prob.spec.residual_fp64 = False
+    t64 = max_over_ranks(f0.elapsed_time(f1) * 1e-3, world, dev)
+    fp64_residual = {"value": whole_job_rate(world, a.steps, t64), "unit": UNIT, "ms_per_step": t64 / a.steps * 1e3,
+                     "pcg_iterations_per_step": its64 / a.steps,
+                     "note": "the timed steps again with gbsimp_solve_opts.residual_fp64 = 1"}
+    prob.restore(state_after)
+
     # ---- roofline of the dominant kernel (the one-kernel PCG iteration) -----------------
     path = prob.eng.apply_path(GRID[2])
     if path == "modal":
@@ -823,11 +846,11 @@ def run_ours(a):
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": tmax / a.steps * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 outer residual, dots, compliance)",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (outer residual in double-float FP32 pairs with FP64 u; compensated FP32 dots; FP64 compliance)",
                 "data": "synthetic", "impl": "ours",
                 "config": dict(WORKLOAD, **_line_keys(world)),
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-                "clocks": clk, "pcg_iterations_per_step": pcg_iters / a.steps,
+                "clocks": clk, "pcg_iterations_per_step": pcg_iters / a.steps, "fp64_residual": fp64_residual,
                 "compliance_rel_err_vs_fp64_oracle": rel_err, "fem_solves_per_s": fem, "c4": c4,
                 "serving": serving, "reference_gpu_path": ref_gpu, "next_rows": rows}
         print(json.dumps(line), flush=True)

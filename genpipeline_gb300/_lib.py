@@ -53,7 +53,7 @@ class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("inner_rtol", C.c_double), ("max_iter", C.c_int32),
                 ("max_outer", C.c_int32), ("check_every", C.c_int32), ("fused", C.c_int32),
                 ("profile", C.c_int32), ("batch_share", C.c_int32), ("batch_group", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("residual_fp64", C.c_int32)]
 
 
 class SolveStats(C.Structure):

@@ -1171,7 +1171,7 @@ static SolveWs solve_ws(void *ws, int nx, int ny, int nz) {
 // orders of magnitude below. Tighter tolerances take the FP64 element pass.
 constexpr double kDdMinRtol = 1e-9;
 static bool use_dd_residual(const gbsimp_ctx *ctx, const gbsimp_solve_opts *o) {
-    return ctx->modal_ok && o->rtol >= kDdMinRtol;
+    return ctx->modal_ok && o->rtol >= kDdMinRtol && !o->residual_fp64;
 }
 
 // r = D f - q (q = D K D u); ||r||^2, ||D f||^2 -> os.

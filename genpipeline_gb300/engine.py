@@ -209,9 +209,9 @@ class Engine:
 
     @staticmethod
     def opts(rtol=1e-8, inner_rtol=1e-4, max_iter=20000, max_outer=20, check_every=0, fused=0,
-             profile=0, batch_share=0, batch_group=0) -> L.SolveOpts:
+             profile=0, batch_share=0, batch_group=0, residual_fp64=0) -> L.SolveOpts:
         return L.SolveOpts(float(rtol), float(inner_rtol), int(max_iter), int(max_outer), int(check_every),
-                           int(fused), int(profile), int(batch_share), int(batch_group), 0)
+                           int(fused), int(profile), int(batch_share), int(batch_group), int(residual_fp64))
 
     def pcg(self, grid: Grid, law: L.Law, x: torch.Tensor, b: torch.Tensor, mask: Optional[torch.Tensor],
             u: torch.Tensor, rtol=1e-6, max_iter=2000, check_every=0, key: str = "pcg", profile=False,
@@ -243,7 +243,7 @@ class Engine:
 
     def solve(self, grid: Grid, law: L.Law, x: torch.Tensor, f: torch.Tensor, mask: Optional[torch.Tensor],
               u: torch.Tensor, rtol=1e-8, inner_rtol=1e-4, max_iter=100000, max_outer=30, check_every=0,
-              key: str = "solve", profile=False, fused=False) -> dict:
+              key: str = "solve", profile=False, fused=False, residual_fp64=False) -> dict:
         nx, ny, nz = grid
         nd = n_dof(grid)
         _need(x, torch.float32, n_elem(grid), "x")
@@ -253,7 +253,8 @@ class Engine:
         ws = self.workspace(key, nb)
         st = L.SolveStats()
         o = self.opts(rtol=rtol, inner_rtol=inner_rtol, max_iter=max_iter, max_outer=max_outer,
-                      check_every=check_every, profile=int(profile), fused=int(fused))
+                      check_every=check_every, profile=int(profile), fused=int(fused),
+                      residual_fp64=int(bool(residual_fp64)))
         L.check(self.lib.gbsimp_solve(self.ctx, nx, ny, nz, C.byref(law), _p(x), _p(f), _p(mask), _p(u), C.byref(o),
                                       C.byref(st), _p(ws), nb, _stream()))
         return st.as_dict()

@@ -42,6 +42,9 @@ class SolveSpec:
     # warm start of solve k >= 3: u_{k-1} + warm_theta (u_{k-1} - u_{k-2}) (0: u_{k-1}); the value
     # of the native loop (gbsimp_simp_run), whose designs this loop reproduces bit for bit
     warm_theta: float = 0.5
+    # 1: the outer residual's element products in FP64 (default: double-float FP32 pairs, whose
+    # rounding is below 1e-12 ||D f||; the FP64 u, the norms and the compliance are FP64 either way)
+    residual_fp64: bool = False
 
     def material(self) -> L.Law:
         return L.make_law(self.law, self.penal, self.e0, self.emin, self.xmin)
@@ -101,7 +104,7 @@ class SimpProblem:
         return self.eng.solve(self.grid, self.law, self.xphys, self.f, self.mask, self.u,
                               rtol=s.rtol if rtol is None else rtol, inner_rtol=s.inner_rtol,
                               max_iter=s.max_iter, max_outer=s.max_outer, key=f"solve:{id(self)}",
-                              profile=self.profile, fused=s.fused)
+                              profile=self.profile, fused=s.fused, residual_fp64=s.residual_fp64)
 
     def step(self) -> dict:
         """One OC iteration of the reference loop."""

@@ -32,7 +32,9 @@ extern "C" {
 #endif
 
 /* 2: gbsimp_solve_opts gained batch_share and batch_group; gbsimp_solve_stats names its two
- * library-owned fields (batched rounds with an iteration budget). */
+ * library-owned fields (batched rounds with an iteration budget). The last field of
+ * gbsimp_solve_opts, reserved (zero) before, selects the FP64 outer residual; zero keeps the
+ * default. */
 #define GBSIMP_ABI_VERSION 2
 
 enum {
@@ -86,7 +88,8 @@ typedef struct gbsimp_solve_opts {
                              grow about with it, so the designs of a launch finish together) */
     int32_t batch_group;  /* batched persistent launches: at most this many designs per launch
                              (0 or more than 24: 24) */
-    int32_t reserved;
+    int32_t residual_fp64; /* 1 = the outer residual's element products in FP64 at every rtol;
+                              0 = in double-float for rtol >= 1e-9 (see gbsimp_solve) */
 } gbsimp_solve_opts;
 
 typedef struct gbsimp_solve_stats {
@@ -233,12 +236,12 @@ size_t gbsimp_time_pcg_apply_ws_bytes(int nx, int ny, int nz);
 int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
                           const float *x, const uint8_t *node_mask, int reps, void *ws,
                           size_t ws_bytes, double *seconds_per_launch, void *stream);
-/* FP32 PCG inner solves with FP64 outer defect correction: r = D(f - K u), FP32 PCG on
- * K d = r to inner_rtol, u += d (FP64), until ||r|| <= rtol ||D f||. u (FP64) holds the warm
- * start on entry. For rtol >= 1e-9 and a modal-form Ke the element products of the residual
- * run in double-float arithmetic (rounding about 2^-46 of the displacement magnitudes of an
- * element; measured below 6.1e-13 ||D f|| on converged fields), the node sums, r and the norms
- * in FP64; for smaller rtol the element products are FP64 too. Synchronises the stream. */
+/* FP32 PCG inner solves with outer defect correction: r = D(f - K u), FP32 PCG on K d = r
+ * to inner_rtol, u += d (FP64), until ||r|| <= rtol ||D f||. u (FP64) holds the warm start on
+ * entry. For rtol >= 1e-9 and a modal-form Ke, unless opts->residual_fp64 is set, the
+ * residual runs in double-float arithmetic (FP32 pairs: rounding about 2^-46 of the
+ * displacement magnitudes of an element, measured below 6.1e-13 ||D f|| on converged fields)
+ * with FP64 u; otherwise its element products are FP64. Synchronises the stream. */
 size_t gbsimp_solve_ws_bytes(int nx, int ny, int nz);
 int gbsimp_solve(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law,
                  const float *x, const double *f, const uint8_t *node_mask, double *u,

@@ -292,6 +292,12 @@ def test_double_float_residual_certifies_fp64(eng, grid, case):
     r = torch.where(fixed_dof, 0.0, fd - y)
     rel64 = (r.norm() / torch.where(fixed_dof, 0.0, fd).norm()).item()
     assert abs(rel64 - st["relres"]) <= 1e-11, (rel64, st["relres"])
+    # the FP64 form on request: the same certificate, to FP64 rounding
+    u2 = torch.zeros_like(u)
+    st2 = eng.solve(grid, lw, xd, _cuda(f), m, u2, rtol=1e-8, residual_fp64=True)
+    assert st2["status"] == L.GBS_OK and st2["relres"] <= 1e-8, st2
+    r2 = torch.where(fixed_dof, 0.0, fd - eng.apply(grid, lw, xd, u2, m))
+    assert abs((r2.norm() / torch.where(fixed_dof, 0.0, fd).norm()).item() - st2["relres"]) <= 1e-13
 
 
 @pytest.mark.parametrize("grid,case", [((12, 6, 6), "cantilever"), ((24, 12, 12), "top_patch")])
