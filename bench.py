@@ -99,7 +99,7 @@ def _spec(w):
     from genpipeline_gb300.simp import SolveSpec
 
     return SolveSpec(grid=tuple(w["grid"]), penal=3.0, rmin=w["rmin"], volfrac=w["volfrac"], law="modified",
-                     rtol=1e-8, inner_rtol=1e-4)
+                     rtol=1e-8)
 
 
 def _load_case(w):

@@ -18,7 +18,7 @@ import torch
 
 from . import _lib as L
 from . import bcs as B
-from .engine import Engine, get_engine, n_dof, n_elem
+from .engine import INNER_RTOL, Engine, get_engine, n_dof, n_elem
 
 
 @dataclass
@@ -56,7 +56,7 @@ class BatchFEM:
     of the designs, the choice cached per grid class)."""
 
     def __init__(self, engine: Optional[Engine] = None, law: Optional[L.Law] = None, rtol: float = 1e-8,
-                 inner_rtol: float = 1e-4, max_iter: int = 200000, max_outer: int = 30, fused: bool = True,
+                 inner_rtol: float = INNER_RTOL, max_iter: int = 200000, max_outer: int = 30, fused: bool = True,
                  round_iters: int = 0, autotune: bool = False, tuner=None):
         self.eng = engine or get_engine()
         self.law = law or L.make_law("modified", 3.0)
@@ -185,7 +185,7 @@ class SolveQueue:
     BatchFEM, with the queue kept by the library."""
 
     def __init__(self, engine: Optional[Engine] = None, law: Optional[L.Law] = None, rtol: float = 1e-8,
-                 inner_rtol: float = 1e-4, max_iter: int = 200000, max_outer: int = 30, fused: bool = True,
+                 inner_rtol: float = INNER_RTOL, max_iter: int = 200000, max_outer: int = 30, fused: bool = True,
                  round_iters: int = 0):
         self.eng = engine or get_engine()
         self.law = law or L.make_law("modified", 3.0)
@@ -235,7 +235,7 @@ class SolveQueue:
 
 
 def solve_plain(designs: List[FEMDesign], engine: Optional[Engine] = None, law: Optional[L.Law] = None,
-                rtol: float = 1e-8, inner_rtol: float = 1e-4) -> List[FEMDesign]:
+                rtol: float = 1e-8, inner_rtol: float = INNER_RTOL) -> List[FEMDesign]:
     """The one-design-at-a-time form: one gbsimp_solve (graph-loop PCG) per design."""
     eng = engine or get_engine()
     law = law or L.make_law("modified", 3.0)

@@ -1170,6 +1170,8 @@ static SolveWs solve_ws(void *ws, int nx, int ny, int nz) {
 // rounding, measured at most 6.1e-13 ||f|| on converged fields (32x16x16, 64^3), stays three
 // orders of magnitude below. Tighter tolerances take the FP64 element pass.
 constexpr double kDdMinRtol = 1e-9;
+// The inner PCG's reduction per outer round when the options leave it at 0 (engine.INNER_RTOL).
+constexpr double kInnerRtol = 3e-5;
 static bool use_dd_residual(const gbsimp_ctx *ctx, const gbsimp_solve_opts *o) {
     return ctx->modal_ok && o->rtol >= kDdMinRtol && !o->residual_fp64;
 }
@@ -1394,7 +1396,7 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
     int total = 0, outer = 0, status = GBS_OK;
     double relres = 0.0;
     const int max_outer = o->max_outer > 0 ? o->max_outer : 20;
-    const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-4;
+    const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : kInnerRtol;
     // Each round: FP64 residual -> one host read (the outer scalars and the previous round's
     // PCG scalars) -> the decisions -> the inner PCG and the correction, enqueued without a
     // host read (the graph loop and the persistent kernel are device-driven).
@@ -1872,7 +1874,7 @@ static int batch_round_impl(const gbsimp_ctx *ctx, gbsimp_batch_item *items, int
                             const gbsimp_solve_opts *o, cudaStream_t st) {
     const Law<float> law = make_law<float>(*glaw);
     const int max_outer = o->max_outer > 0 ? o->max_outer : 20;
-    const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : 1e-4;
+    const double inner = o->inner_rtol > 0.0 ? o->inner_rtol : kInnerRtol;
     // iteration budget of the inner PCGs in this round (0: each runs to its tolerance)
     const int budget = o->check_every > 0 ? o->check_every : 0;
     const bool dd = use_dd_residual(ctx, o);

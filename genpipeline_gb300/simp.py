@@ -18,7 +18,7 @@ import torch
 
 from . import _lib as L
 from . import bcs as B
-from .engine import Engine, get_engine, n_dof, n_elem
+from .engine import INNER_RTOL, Engine, get_engine, n_dof, n_elem
 
 
 @dataclass
@@ -35,7 +35,7 @@ class SolveSpec:
     xmin: float = 1e-3
     oc_variant: dict = field(default_factory=lambda: dict(L.OC_CPU))
     rtol: float = 1e-8          # FP64 outer residual target
-    inner_rtol: float = 1e-4    # FP32 PCG reduction per outer correction (FP32 stagnates below ~1e-5)
+    inner_rtol: float = INNER_RTOL  # FP32 PCG reduction per outer correction (engine.INNER_RTOL)
     max_iter: int = 200000
     max_outer: int = 30
     fused: bool = False         # persistent one-launch PCG (grid barriers) instead of the graph loop

@@ -71,7 +71,7 @@ typedef struct gbsimp_oc_params {
 /* Options and results of the linear solves. */
 typedef struct gbsimp_solve_opts {
     double rtol;          /* stop when ||D(f - K u)|| <= rtol * ||D f|| (outer residual, see gbsimp_solve) */
-    double inner_rtol;    /* FP32 PCG reduction per outer correction (gbsimp_solve, batch); <= 0: 1e-4 */
+    double inner_rtol;    /* FP32 PCG reduction per outer correction (gbsimp_solve, batch); <= 0: 3e-5 */
     int32_t max_iter;     /* cap on the total FP32 PCG iterations */
     int32_t max_outer;    /* cap on outer defect corrections (gbsimp_solve, batched rounds) */
     int32_t check_every;  /* iterations between the host's checks where the host drives the
