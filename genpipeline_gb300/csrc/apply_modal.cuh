@@ -775,10 +775,37 @@ __device__ __forceinline__ void cg_scalar_step_df(df32 gamma, df32 delta, df32 r
     }
 }
 
+// The scalars of iteration 0 from the sums of a start pass (alpha = beta = 0 from x0 = 0:
+// gamma = r_0.u_0, delta = w_0.u_0, rho = r_0.r_0 = ||D b||^2): alpha_0 = gamma / delta,
+// beta_0 = 0. Stops at once on a non-finite sum, on D b = 0, or when rtol > 1 (x0 = 0 already
+// meets ||r|| < rtol ||D b||); breakdown when delta is not positive.
+__device__ __forceinline__ void cg_first_step_df(df32 gamma, df32 delta, df32 rho, double tol, int &done,
+                                                 int &status, df32 &gamma_i, df32 &alpha, df32 &beta) {
+    if (!isfinite(gamma.hi) || !isfinite(delta.hi) || !isfinite(rho.hi)) {
+        done = 1;
+        status = GBS_ENONFINITE;
+    } else if (rho.hi == 0.0f || tol > 1.0) {
+        done = 1;
+    } else if (!(delta.hi > 0.0f)) {
+        done = 1;
+        status = GBS_EBREAKDOWN;
+    } else {
+        alpha = df_div(gamma, delta);
+        beta = df32{0.0f, 0.0f};
+        gamma_i = gamma;
+    }
+}
+
+// CgState.pending: the sums of the pass that wrote the state are still to be folded (1); the
+// same for a start pass (2: cg_first_step_df instead of the scalar step); the next launch is
+// the start pass itself (3: nothing to fold, it runs with alpha = beta = 0).
+enum { CG_PENDING_STEP = 1, CG_PENDING_FIRST = 2, CG_START_PASS = 3 };
+
 // Folds the block partial sums (r.u, w.u, r.r; double-float, slot layout [k][nblk]) of the
-// pass that started from state s into s: the scalar step of that iteration. Every block of the
-// next launch does it, in the same order (deterministic), instead of a last block of the pass.
-// All threads of the block take part; nothing runs on the FP64 pipe.
+// pass that started from state s into s: the scalar step of that iteration (of a start pass:
+// the scalars of iteration 0). Every block of the next launch does it, in the same order
+// (deterministic), instead of a last block of the pass. All threads of the block take part;
+// nothing runs on the FP64 pipe.
 template <int NT>
 __device__ __forceinline__ void cg_fold(CgState &s, const PcgScalars *sc, const float2 *partials, int nblk,
                                         float2 *sred) {
@@ -794,8 +821,11 @@ __device__ __forceinline__ void cg_fold(CgState &s, const PcgScalars *sc, const 
     if (threadIdx.x == 0) {
         int it = s.iter, done = 0, status = s.status;
         const df32 a_before = s.alpha;
-        cg_scalar_step_df(tot[0], tot[1], tot[2], sc->rr_stop, sc->max_iter, it, done, status, s.gamma, s.alpha,
-                          s.beta);
+        if (s.pending == CG_PENDING_FIRST)
+            cg_first_step_df(tot[0], tot[1], tot[2], sc->tol, done, status, s.gamma, s.alpha, s.beta);
+        else
+            cg_scalar_step_df(tot[0], tot[1], tot[2], sc->rr_stop, sc->max_iter, it, done, status, s.gamma,
+                              s.alpha, s.beta);
         if (!done) s.alpha_prev = a_before;
         s.iter = it;
         s.done = done;
@@ -844,11 +874,20 @@ __global__ void __launch_bounds__(NT, 2)
         const PcgScalars *sc = ca.sc;
         CgState s = sc->st[par ^ 1];
         if (!sc->freeze) {
-            if (s.pending && !s.done)
+            const int pend = s.pending;
+            if ((pend == CG_PENDING_STEP || pend == CG_PENDING_FIRST) && !s.done) {
                 cg_fold<NT>(s, sc, (const float2 *)ca.partials + (par ^ 1) * 3 * nblk, nblk, sred);
+                if (pend == CG_PENDING_FIRST && bid == 0 && tid == 0) {
+                    // the stop threshold (rtol ||D b||)^2 of the later folds, ||D b||^2 = r_0.r_0
+                    const double bn = sqrt(df_value(s.rr));
+                    const double stop = sc->tol * bn;
+                    ca.sc->bnorm = bn;
+                    ca.sc->rr_stop = (float)(stop * stop);
+                }
+            }
             if (bid == 0 && tid == 0) {
                 CgState o = s;
-                o.pending = s.done ? 0 : 1;
+                o.pending = s.done ? 0 : (pend == CG_START_PASS ? CG_PENDING_FIRST : CG_PENDING_STEP);
                 ca.sc->st[par] = o;
             }
         }

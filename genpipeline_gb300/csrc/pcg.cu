@@ -369,8 +369,11 @@ __global__ void cg_start_kernel(int64_t nd, const float *__restrict__ w, const f
 __global__ void cg_fold_kernel(int nblk, int last, double *partials, PcgScalars *sc) {
     __shared__ float2 sred[3 * 32];
     CgState s = sc->st[last];
-    if (s.pending && !s.done) cg_fold<256>(s, sc, (const float2 *)partials + last * 3 * nblk, nblk, sred);
+    const int pend = s.pending;
+    if ((pend == CG_PENDING_STEP || pend == CG_PENDING_FIRST) && !s.done)
+        cg_fold<256>(s, sc, (const float2 *)partials + last * 3 * nblk, nblk, sred);
     if (threadIdx.x == 0) {
+        if (pend == CG_PENDING_FIRST) sc->bnorm = sqrt(df_value(s.rr));
         sc->st[last] = s;
         sc->iter = s.iter;
         sc->rz = df_value(s.gamma);
@@ -950,6 +953,51 @@ static int launch_loop_graph(const gbsimp_ctx *ctx, int nx, int ny, int nz, cons
 // the workspace is already that of this x and mask (an earlier round of the same solve).
 enum { SETUP_X0_ZERO = 1, SETUP_KEEP_DINV = 2 };
 
+// 1/diag of K(x) on free DOFs and, for the modal kernels, the element moduli E(x_e).
+static int setup_diag(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<float> &law, const float *x,
+                      const uint8_t *mask, const PcgWs &w, cudaStream_t st) {
+    const int64_t nd = n_dof_of(nx, ny, nz);
+    dinv_kernel<float><<<ew_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, fast_div(ny + 1), fast_div(nz + 1), law,
+                                                                 ctx->kef, x, mask, w.dinv);
+    GBS_LAUNCH_CHECK("dinv_kernel");
+    if (use_modal(ctx, nz)) {
+        const int64_t ne = (int64_t)nx * ny * nz;
+        moduli_f32_kernel<<<ew_blocks(ctx, ne), 256, 0, st>>>(ne, law, x, w.E);
+        GBS_LAUNCH_CHECK("moduli_f32_kernel");
+    }
+    return GBS_OK;
+}
+
+// Start of a one-kernel PCG from x0 = 0 without a setup apply. r_0 = D b on free DOFs goes to
+// the r buffer of the start pass (an odd launch, phase 5); x, p, the s it reads, the w it
+// reads and the w it adds its output into are zeroed; the scalars are reset with the state
+// marked CG_START_PASS. The start pass (alpha = beta = 0) then forms u_0 = M r_0,
+// w_0 = D K D u_0 and the sums r_0.u_0, w_0.u_0, r_0.r_0, and the launch after it folds them
+// into alpha_0 and the stop threshold (cg_first_step_df).
+__global__ void cg_fresh_kernel(int64_t nd, const float *__restrict__ b, const uint8_t *__restrict__ mask, float *r,
+                                float *p, float *sold, float *w_in, float *w_out, float *x, PcgScalars *sc, double tol,
+                                int max_iter, int max_trips) {
+    for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
+        r[d] = dof_fixed(mask, d) ? 0.0f : b[d];
+        p[d] = 0.0f;
+        sold[d] = 0.0f;
+        w_in[d] = 0.0f;
+        w_out[d] = 0.0f;
+        x[d] = 0.0f;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        PcgScalars z = {};
+        z.tol = tol;
+        z.max_iter = max_iter;
+        z.max_trips = max_trips;
+        z.status = GBS_OK;
+        z.st[0].pending = CG_START_PASS;
+        z.st[0].status = GBS_OK;
+        *sc = z;
+    }
+}
+
+
 // PCG setup on the stream: zeroed scalars, 1/diag, q = D K D u, r = D b - q, then for the
 // single-reduction form u_0 = M r_0, w_0 = D K D u_0 and alpha_0, for the dense form
 // p_{-1} = 0; the first dot products and the stop test (nothing is read back).
@@ -964,14 +1012,8 @@ static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp
     }
     GBS_CUDA_TRY(cudaMemsetAsync(w.sc, 0, sizeof(PcgScalars), st));
     if (!(flags & SETUP_KEEP_DINV)) {
-        dinv_kernel<float><<<ew_blocks(ctx, nd / 3), 256, 0, st>>>(nx, ny, nz, fast_div(ny + 1), fast_div(nz + 1), law,
-                                                                     ctx->kef, x, mask, w.dinv);
-        GBS_LAUNCH_CHECK("dinv_kernel");
-        if (use_modal(ctx, nz)) {
-            const int64_t ne = (int64_t)nx * ny * nz;
-            moduli_f32_kernel<<<ew_blocks(ctx, ne), 256, 0, st>>>(ne, law, x, w.E);
-            GBS_LAUNCH_CHECK("moduli_f32_kernel");
-        }
+        const int rc = setup_diag(ctx, nx, ny, nz, law, x, mask, w, st);
+        if (rc) return rc;
     }
     const int max_trips = (max_iter + kLoopUnroll - 1) / kLoopUnroll + 2;
     // q = D K D u into `qbuf`, or zeros when u is known to be zero
@@ -1009,6 +1051,28 @@ static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp
     return GBS_OK;
 }
 
+// pcg_setup for the one-kernel PCG from x0 = 0 (max_iter > 0): cg_fresh_kernel and the start
+// pass, two launches instead of the setup's reductions and apply.
+static int pcg_fresh_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x,
+                           const float *b, const uint8_t *mask, float *u, double rtol, int max_iter, const PcgWs &w,
+                           cudaStream_t st, unsigned flags) {
+    const int64_t nd = n_dof_of(nx, ny, nz);
+    const Law<float> law = make_law<float>(*glaw);
+    int rc = check_modal_partials(ctx, nx, ny, nz, w);
+    if (rc) return rc;
+    if (!(flags & SETUP_KEEP_DINV)) {
+        rc = setup_diag(ctx, nx, ny, nz, law, x, mask, w, st);
+        if (rc) return rc;
+    }
+    const int max_trips = (max_iter + kLoopUnroll - 1) / kLoopUnroll + 2;
+    const CgArgs ca = cg_args(w, u);
+    // phase 5 reads r[1], s[0], w[2] and adds into w[0] (the launch that precedes phase 0)
+    cg_fresh_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, b, mask, ca.r[1], ca.p, ca.s[0], ca.w[2], ca.w[0], u, w.sc,
+                                                         rtol, max_iter, max_trips);
+    GBS_LAUNCH_CHECK("cg_fresh_kernel");
+    return pcg_iteration(ctx, nx, ny, nz, law, x, mask, u, w, st, nullptr, 5);
+}
+
 // Optional profiling (prof != nullptr): CUDA events around every K1 launch; only the
 // launches of iterations that actually ran (the device counter advanced) are summed.
 struct ApplyProfile {
@@ -1026,7 +1090,11 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
     const int64_t nd = n_dof_of(nx, ny, nz);
     PcgWs w = pcg_ws(ws, nx, ny, nz);
     const Law<float> law = make_law<float>(*glaw);
-    int rc = pcg_setup(ctx, nx, ny, nz, glaw, x, b, mask, u, rtol, max_iter, w, st, setup_flags);
+    // from x0 = 0 the one-kernel form starts with a start pass instead of the setup's apply
+    // (the persistent kernel keeps the setup: it reads the scalars of iteration 0)
+    const bool fresh = use_modal(ctx, nz) && (setup_flags & SETUP_X0_ZERO) && !fused && max_iter > 0;
+    int rc = fresh ? pcg_fresh_setup(ctx, nx, ny, nz, glaw, x, b, mask, u, rtol, max_iter, w, st, setup_flags)
+                   : pcg_setup(ctx, nx, ny, nz, glaw, x, b, mask, u, rtol, max_iter, w, st, setup_flags);
     if (rc) return rc;
     PcgScalars h;
     memset(&h, 0, sizeof h);
