@@ -974,11 +974,22 @@ static int setup_diag(const gbsimp_ctx *ctx, int nx, int ny, int nz, const Law<f
 // marked CG_START_PASS. The start pass (alpha = beta = 0) then forms u_0 = M r_0,
 // w_0 = D K D u_0 and the sums r_0.u_0, w_0.u_0, r_0.r_0, and the launch after it folds them
 // into alpha_0 and the stop threshold (cg_first_step_df).
-__global__ void cg_fresh_kernel(int64_t nd, const float *__restrict__ b, const uint8_t *__restrict__ mask, float *r,
-                                float *p, float *sold, float *w_in, float *w_out, float *x, PcgScalars *sc, double tol,
-                                int max_iter, int max_trips) {
+// The right-hand side is b, or with bdd given (h, l) pairs scaled by *bscale in FP32 (the
+// outer residual r / ||r|| formed here instead of by a separate scale pass).
+__global__ void cg_fresh_kernel(int64_t nd, const float *__restrict__ b, const float2 *__restrict__ bdd,
+                                const double *bscale, const uint8_t *__restrict__ mask, float *r, float *p, float *sold,
+                                float *w_in, float *w_out, float *x, PcgScalars *sc, double tol, int max_iter,
+                                int max_trips) {
+    const float bs = bdd ? (float)*bscale : 0.0f;
     for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
-        r[d] = dof_fixed(mask, d) ? 0.0f : b[d];
+        float bv;
+        if (bdd) {
+            const float2 v = bdd[d];
+            bv = fmaf(v.x, bs, v.y * bs);
+        } else {
+            bv = b[d];
+        }
+        r[d] = dof_fixed(mask, d) ? 0.0f : bv;
         p[d] = 0.0f;
         sold[d] = 0.0f;
         w_in[d] = 0.0f;
@@ -1051,11 +1062,16 @@ static int pcg_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp
     return GBS_OK;
 }
 
+// Whether pcg_run starts this solve with pcg_fresh_setup.
+static inline bool fresh_start_ok(const gbsimp_ctx *ctx, int nz, int fused, int max_iter, unsigned flags) {
+    return use_modal(ctx, nz) && (flags & SETUP_X0_ZERO) && !fused && max_iter > 0;
+}
+
 // pcg_setup for the one-kernel PCG from x0 = 0 (max_iter > 0): cg_fresh_kernel and the start
 // pass, two launches instead of the setup's reductions and apply.
 static int pcg_fresh_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x,
-                           const float *b, const uint8_t *mask, float *u, double rtol, int max_iter, const PcgWs &w,
-                           cudaStream_t st, unsigned flags) {
+                           const float *b, const float2 *bdd, const double *bscale, const uint8_t *mask, float *u,
+                           double rtol, int max_iter, const PcgWs &w, cudaStream_t st, unsigned flags) {
     const int64_t nd = n_dof_of(nx, ny, nz);
     const Law<float> law = make_law<float>(*glaw);
     int rc = check_modal_partials(ctx, nx, ny, nz, w);
@@ -1067,8 +1083,8 @@ static int pcg_fresh_setup(const gbsimp_ctx *ctx, int nx, int ny, int nz, const 
     const int max_trips = (max_iter + kLoopUnroll - 1) / kLoopUnroll + 2;
     const CgArgs ca = cg_args(w, u);
     // phase 5 reads r[1], s[0], w[2] and adds into w[0] (the launch that precedes phase 0)
-    cg_fresh_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, b, mask, ca.r[1], ca.p, ca.s[0], ca.w[2], ca.w[0], u, w.sc,
-                                                         rtol, max_iter, max_trips);
+    cg_fresh_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, b, bdd, bscale, mask, ca.r[1], ca.p, ca.s[0], ca.w[2],
+                                                         ca.w[0], u, w.sc, rtol, max_iter, max_trips);
     GBS_LAUNCH_CHECK("cg_fresh_kernel");
     return pcg_iteration(ctx, nx, ny, nz, law, x, mask, u, w, st, nullptr, 5);
 }
@@ -1086,14 +1102,18 @@ struct ApplyProfile {
 // together with its own.
 int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x, const float *b,
             const uint8_t *mask, float *u, double rtol, int max_iter, int check_every, void *ws, PcgScalars *out,
-            cudaStream_t st, ApplyProfile *prof = nullptr, int fused = 0, unsigned setup_flags = 0) {
+            cudaStream_t st, ApplyProfile *prof = nullptr, int fused = 0, unsigned setup_flags = 0,
+            const float2 *bdd = nullptr, const double *bscale = nullptr) {
     const int64_t nd = n_dof_of(nx, ny, nz);
     PcgWs w = pcg_ws(ws, nx, ny, nz);
     const Law<float> law = make_law<float>(*glaw);
     // from x0 = 0 the one-kernel form starts with a start pass instead of the setup's apply
-    // (the persistent kernel keeps the setup: it reads the scalars of iteration 0)
-    const bool fresh = use_modal(ctx, nz) && (setup_flags & SETUP_X0_ZERO) && !fused && max_iter > 0;
-    int rc = fresh ? pcg_fresh_setup(ctx, nx, ny, nz, glaw, x, b, mask, u, rtol, max_iter, w, st, setup_flags)
+    // (the persistent kernel keeps the setup: it reads the scalars of iteration 0); only this
+    // start takes the right-hand side as scaled (h, l) pairs
+    const bool fresh = fresh_start_ok(ctx, nz, fused, max_iter, setup_flags);
+    if (bdd && !fresh) return set_error(GBS_EINVAL, "pcg_run: a (h, l) right-hand side needs the fresh start");
+    int rc = fresh ? pcg_fresh_setup(ctx, nx, ny, nz, glaw, x, b, bdd, bscale, mask, u, rtol, max_iter, w, st,
+                                     setup_flags)
                    : pcg_setup(ctx, nx, ny, nz, glaw, x, b, mask, u, rtol, max_iter, w, st, setup_flags);
     if (rc) return rc;
     PcgScalars h;
@@ -1509,15 +1529,20 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
             status = GBS_ENOTCONV;
             break;
         }
-        rc = outer_scale(ctx, nd, dd, w, st);
-        if (rc) return rc;
+        // the first round computes 1/diag, later rounds reuse it
+        const unsigned flags = SETUP_X0_ZERO | (outer > 1 ? SETUP_KEEP_DINV : 0u);
+        // the fresh start forms b = r / ||r|| itself from the double-float residual
+        const bool scaled_in_start = dd && fresh_start_ok(ctx, nz, o->fused, o->max_iter - total, flags);
+        if (!scaled_in_start) {
+            rc = outer_scale(ctx, nd, dd, w, st);
+            if (rc) return rc;
+        }
         // Inner tolerance: enough to reach rtol from here, but not below what FP32 resolves.
         double itol = o->rtol / relres;
         if (itol < inner) itol = inner;
-        // d32 was zeroed above; the first round computes 1/diag, later rounds reuse it
         rc = pcg_run(ctx, nx, ny, nz, law, x, w.b32, mask, w.d32, itol, o->max_iter - total, o->check_every, w.pcg,
-                     async ? nullptr : &ps, st, o->profile ? &prof : nullptr, o->fused,
-                     SETUP_X0_ZERO | (outer > 1 ? SETUP_KEEP_DINV : 0u));
+                     async ? nullptr : &ps, st, o->profile ? &prof : nullptr, o->fused, flags,
+                     scaled_in_start ? (const float2 *)w.r64 : nullptr, scaled_in_start ? &w.os->scale : nullptr);
         if (rc) return rc;
         if (async) {
             pending = pw.sc;
