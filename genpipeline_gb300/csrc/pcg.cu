@@ -1289,9 +1289,10 @@ __global__ void resid64_kernel(int64_t nd, const double *__restrict__ f, const d
 // element pass summed in the fixed order b = 0..7 (double-float), then r = D(f - q) in FP64
 // and ||r||^2, ||D f||^2 -> os.
 // Once per solve, before the first double-float residual: fdd = the split of D f, and
-// ||D f||^2 (FP64, from f itself) with sigma = 2^-round(log2 ||D f||).
+// ||D f||^2 (FP64, from f itself) with sigma = 2^-round(log2 ||D f||); udd = the split of the
+// start vector u (fixed DOFs zero).
 __global__ void split_f_kernel(int64_t nd, const double *__restrict__ f, const uint8_t *__restrict__ mask, float2 *fdd,
-                               double *partials, OuterScalars *os) {
+                               double *partials, OuterScalars *os, const double *__restrict__ u, float2 *udd) {
     double ff = 0.0;
     for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < nd; d += (int64_t)gridDim.x * blockDim.x) {
         const bool fx = dof_fixed(mask, d);
@@ -1299,6 +1300,8 @@ __global__ void split_f_kernel(int64_t nd, const double *__restrict__ f, const u
         const ddv s = fx ? ddv{0.0f, 0.0f} : dd_split(v);
         fdd[d] = make_float2(s.h, s.l);
         ff = fma(v, v, ff);
+        const ddv us = fx ? ddv{0.0f, 0.0f} : dd_split(u[d]);
+        udd[d] = make_float2(us.h, us.l);
     }
     __shared__ double tot[3];
     const ddv fs = dd_split(ff);  // the thread's FP64 partial, summed on in double-float
@@ -1434,13 +1437,12 @@ static int outer_correct(const gbsimp_ctx *ctx, int64_t nd, const uint8_t *mask,
     return GBS_OK;
 }
 
-// Before the first residual of a solve: the double-float splits of u and D f, ||D f||^2.
+// Before the first residual of a solve: the double-float splits of u and D f, ||D f||^2 (one
+// pass).
 static int outer_start(const gbsimp_ctx *ctx, int64_t nd, const double *u, const double *f, const uint8_t *mask,
                        bool dd, const SolveWs &w, cudaStream_t st) {
     if (!dd) return GBS_OK;
-    int rc = split_dd(ctx, nd, u, mask, w.udd, st);
-    if (rc) return rc;
-    split_f_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, f, mask, w.fdd, w.partials, w.os);
+    split_f_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, f, mask, w.fdd, w.partials, w.os, u, w.udd);
     GBS_LAUNCH_CHECK("split_f_kernel");
     return GBS_OK;
 }
