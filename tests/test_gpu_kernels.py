@@ -412,6 +412,27 @@ def test_solve_warm_start_and_zero_load(eng):
     assert s3["status"] == L.GBS_OK and torch.count_nonzero(uz).item() == 0
 
 
+@pytest.mark.parametrize("fused", [False, True])
+def test_solve_inner_start_stop_rules(eng, fused):
+    """The inner solves of the graph loop start with a start pass whose sums the next launch
+    folds into alpha_0 (the persistent form keeps the setup kernels); both stop the same way.
+    An iteration cap of 5 ends the inner solve after exactly 5 iterations and the outer loop
+    with ENOTCONV; an inner tolerance above 1 is met by x0 = 0 at once, so no iteration runs,
+    u stays zero and the outer loop ends at its round cap."""
+    grid = (12, 6, 6)
+    f, fixed, x = _problem(grid)
+    m = _cuda(bcs.node_mask(*grid, fixed))
+    lw = L.make_law("modified", 3.0)
+    u = torch.zeros(n_dof(grid), dtype=torch.float64, device="cuda")
+    st = eng.solve(grid, lw, _cuda(x), _cuda(f), m, u, max_iter=5, fused=fused)
+    assert st["status"] == L.GBS_ENOTCONV and st["iterations"] == 5, st
+    assert 0.0 < st["relres"] < 1.0 and torch.isfinite(u).all()
+    u.zero_()
+    st = eng.solve(grid, lw, _cuda(x), _cuda(f), m, u, inner_rtol=2.0, max_outer=3, fused=fused)
+    assert st["status"] == L.GBS_ENOTCONV and st["iterations"] == 0, st
+    assert torch.count_nonzero(u).item() == 0
+
+
 def test_pcg_breakdown_and_cap_are_statuses(eng):
     grid = (8, 4, 4)
     f, fixed, x = _problem(grid)
