@@ -12,8 +12,8 @@ filtered dc, x and xPhys and solves stopped at rtol 1e-8. Measured drift of that
     64^3, 100 it., modified       3.8e-8                1.2e-7         identical
 
 The GPU path adds FP32 rounding of its own arithmetic (filter sums, OC update) on top of
-that. Measured on a GB300: 1.2e-7 / 1.4e-6 (32x16x16 modified), 1.2e-7 / 1.9e-6 (32x16x16
-reference law) and 4.8e-8 / 4.5e-7 (64^3), with identical bisection step counts: the drift
+that. Measured on a GB300: 1.4e-7 / 1.4e-6 (32x16x16 modified), 1.2e-7 / 1.1e-6 (32x16x16
+reference law) and 3.8e-8 / 4.5e-7 (64^3), with identical bisection step counts: the drift
 floor itself. The bounds below are the target's 1e-6 on compliance and 1e-5 on any density.
 
 ``SIMPSolverGPU.run`` and ``BatchSIMP`` are compared with ``oracle.simp_gpu_run``, the
