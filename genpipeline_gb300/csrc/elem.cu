@@ -764,6 +764,7 @@ extern "C" size_t gbsimp_sensitivity_ws_bytes(int nx, int ny, int nz) {
 extern "C" int gbsimp_sensitivity(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *law, const float *x,
                                   const double *u, float *dc, float *ce, double *energy_out, void *ws,
                                   size_t ws_bytes, void *stream) {
+    NvtxRange range("gbsimp_sensitivity");
     if (!ctx || !law || !x || !u || !grid_ok(nx, ny, nz))
         return set_error(GBS_EINVAL, "gbsimp_sensitivity: bad arguments");
     if (energy_out && (!ws || ws_bytes < reduce_ws_bytes(4096)))
@@ -799,6 +800,7 @@ extern "C" int gbsimp_filter_hs(gbsimp_ctx *ctx, int nx, int ny, int nz, double 
 
 extern "C" int gbsimp_filter(gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const float *hs, const float *in,
                              float *out, int transpose, void *stream) {
+    NvtxRange range("gbsimp_filter");
     if (!ctx || !in || !out || !grid_ok(nx, ny, nz))
         return set_error(GBS_EINVAL, "gbsimp_filter: bad arguments");
     if (transpose && !hs) return set_error(GBS_EINVAL, "gbsimp_filter: the transpose needs hs");
@@ -853,6 +855,7 @@ static int oc_coop_blocks(const gbsimp_ctx *ctx) {
 
 int oc_run_impl(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, const gbsimp_oc_params *prm, const float *x,
                 const float *dc, const uint8_t *preserved, float *xnew, float *xphys, void *ws, cudaStream_t st) {
+    NvtxRange range("OC update");
     const int64_t n = (int64_t)nx * ny * nz;
     OcWs w = oc_ws(ws, n);
     OcParams P;

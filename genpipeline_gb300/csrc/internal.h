@@ -1,9 +1,21 @@
 // internal.h -- functions shared between the translation units of libgbsimp.
 #pragma once
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "common.cuh"
 
 namespace gbs {
+// A named NVTX range over a host scope: each phase of a SIMP iteration (solve with its outer
+// rounds and inner PCGs, sensitivity, filter, OC update) shows as a span in a profiler's
+// timeline. NVTX is header-only; with no tool attached a range costs one call.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 // Grids the kernels accept: positive extents and DOF indices that fit in 32 bits
 // (3 (nx+1)(ny+1)(nz+1) < 2^31; node and DOF offsets are 32-bit in places). Each extent is
 // widened before the +1 and bounded before the products, so no int or int64 arithmetic

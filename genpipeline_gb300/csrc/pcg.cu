@@ -153,12 +153,19 @@ __global__ void dinv_kernel(int nx, int ny, int nz, const FastDiv fNY, const Fas
     for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
         int i, j, k;
         unflatten3((uint32_t)n, fNY, fNZ, i, j, k);
-        T acc[3] = {0, 0, 0};
+        // the 8 density loads first; an element outside the grid adds an exact zero
+        float xe[8];
+        bool in[8];
 #pragma unroll
         for (int a = 0; a < 8; ++a) {
             const int ei = i - corner_x(a), ej = j - corner_y(a), ek = k - corner_z(a);
-            if (ei < 0 || ej < 0 || ek < 0 || ei >= nx || ej >= ny || ek >= nz) continue;
-            const T E = modulus(law, (T)x[((int64_t)ei * ny + ej) * nz + ek]);
+            in[a] = ei >= 0 && ej >= 0 && ek >= 0 && ei < nx && ej < ny && ek < nz;
+            xe[a] = in[a] ? x[((int64_t)ei * ny + ej) * nz + ek] : 0.0f;
+        }
+        T acc[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            const T E = in[a] ? modulus(law, (T)xe[a]) : (T)0;
 #pragma unroll
             for (int c = 0; c < 3; ++c) acc[c] += E * (T)kd.k[(3 * a + c) * 25];
         }
@@ -1327,19 +1334,23 @@ __global__ void __launch_bounds__(256) resid_dd_kernel(int nx, int ny, int nz, c
     for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < n_nodes; n += (int64_t)gridDim.x * blockDim.x) {
         int i, j, k;
         unflatten3((uint32_t)n, fNY, fNZ, i, j, k);
-        ddv acc[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+        // all 24 loads first (zero outside the grid: adding an exact zero leaves a pair as it
+        // is), then the sums in the fixed order b = 0..7
+        float2 w[8][3];
 #pragma unroll
         for (int b = 0; b < 8; ++b) {
             const int ei = i - (b >> 2), ej = j - ((b >> 1) & 1), ek = k - (b & 1);
-            if (ei < 0 || ej < 0 || ek < 0 || ei >= nx || ej >= ny || ek >= nz) continue;
-            const int64_t e = ((int64_t)ei * ny + ej) * nz + ek;
+            const bool in = ei >= 0 && ej >= 0 && ek >= 0 && ei < nx && ej < ny && ek < nz;
+            const int64_t e = in ? ((int64_t)ei * ny + ej) * nz + ek : 0;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float2 w = C[(b * 3 + c) * n_elem + e];
-                acc[c] = dd_add(acc[c], ddv{w.x, w.y});
-            }
+            for (int c = 0; c < 3; ++c) w[b][c] = in ? __ldg(&C[(b * 3 + c) * n_elem + e]) : make_float2(0.0f, 0.0f);
         }
         const uint8_t m = mask ? mask[n] : (uint8_t)0;
+        ddv acc[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+#pragma unroll
+        for (int b = 0; b < 8; ++b)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) acc[c] = dd_add(acc[c], ddv{w[b][c].x, w[b][c].y});
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const bool fx = (m >> c) & 1;
@@ -1499,12 +1510,16 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
         if (rc) return rc;
     }
     for (;;) {
-        int rc = outer_residual(ctx, nx, ny, nz, law, x, f, mask, u, dd, w, st);
-        if (rc) return rc;
         OuterScalars h;
         PcgScalars ps;
-        rc = read_outer(w.os, &h, pending, &ps, st);
-        if (rc) return rc;
+        {
+            NvtxRange range("outer residual");
+            int rc = outer_residual(ctx, nx, ny, nz, law, x, f, mask, u, dd, w, st);
+            if (rc) return rc;
+            rc = read_outer(w.os, &h, pending, &ps, st);
+            if (rc) return rc;
+        }
+        int rc = GBS_OK;
         ++outer;
         if (pending) {
             pending = nullptr;
@@ -1542,9 +1557,12 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
         // Inner tolerance: enough to reach rtol from here, but not below what FP32 resolves.
         double itol = o->rtol / relres;
         if (itol < inner) itol = inner;
-        rc = pcg_run(ctx, nx, ny, nz, law, x, w.b32, mask, w.d32, itol, o->max_iter - total, o->check_every, w.pcg,
-                     async ? nullptr : &ps, st, o->profile ? &prof : nullptr, o->fused, flags,
-                     scaled_in_start ? (const float2 *)w.r64 : nullptr, scaled_in_start ? &w.os->scale : nullptr);
+        {
+            NvtxRange range("inner PCG");
+            rc = pcg_run(ctx, nx, ny, nz, law, x, w.b32, mask, w.d32, itol, o->max_iter - total, o->check_every, w.pcg,
+                         async ? nullptr : &ps, st, o->profile ? &prof : nullptr, o->fused, flags,
+                         scaled_in_start ? (const float2 *)w.r64 : nullptr, scaled_in_start ? &w.os->scale : nullptr);
+        }
         if (rc) return rc;
         if (async) {
             pending = pw.sc;
@@ -1878,6 +1896,7 @@ extern "C" int gbsimp_pcg_f32(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbs
 
 extern "C" int gbsimp_warm_start(gbsimp_ctx *ctx, int64_t n, double *u, double *u_prev, double theta,
                                  void *stream) {
+    NvtxRange range("gbsimp_warm_start");
     if (!ctx || n < 0 || (n > 0 && (!u || !u_prev)) || !isfinite(theta))
         return set_error(GBS_EINVAL, "gbsimp_warm_start: bad arguments");
     return warm_start_impl(ctx, n, u, u_prev, theta, (cudaStream_t)stream);
@@ -1889,6 +1908,7 @@ extern "C" int gbsimp_solve(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsim
     auto t0 = std::chrono::steady_clock::now();
     if (!ctx || !law || !x || !f || !u || !opts || !ws || !grid_ok(nx, ny, nz))
         return set_error(GBS_EINVAL, "gbsimp_solve: bad arguments");
+    NvtxRange range("gbsimp_solve");
     if (ws_bytes < solve_ws_bytes_impl(nx, ny, nz)) return set_error(GBS_EINVAL, "gbsimp_solve: workspace too small");
     gbsimp_solve_stats s{};
     int rc = solve_run(ctx, nx, ny, nz, law, x, f, node_mask, u, opts, &s, ws, (cudaStream_t)stream);
@@ -2191,6 +2211,7 @@ static int check_batch(gbsimp_ctx *ctx, gbsimp_batch_item *items, int n, const g
 
 extern "C" int gbsimp_batch_round(gbsimp_ctx *ctx, gbsimp_batch_item *items, int n, const gbsimp_law *law,
                                   const gbsimp_solve_opts *opts, void *stream) {
+    NvtxRange range("gbsimp_batch_round");
     int rc = check_batch(ctx, items, n, law, opts);
     if (rc) return rc;
     return batch_round_impl(ctx, items, n, law, opts, (cudaStream_t)stream);

@@ -76,6 +76,7 @@ extern "C" int gbsimp_simp_run(gbsimp_ctx *ctx, int nx, int ny, int nz, const gb
                                const uint8_t *preserved, float *x, float *xphys, double *u, double *compliance,
                                int32_t *iters_out, gbsimp_solve_stats *last_stats, void *ws, size_t ws_bytes,
                                void *stream) {
+    NvtxRange range("gbsimp_simp_run");
     if (!ctx || !law || !opts || !f || !x || !xphys || !u || !ws || nx <= 0 || ny <= 0 || nz <= 0)
         return set_error(GBS_EINVAL, "gbsimp_simp_run: bad arguments");
     if (opts->n_iters < 0 || !(opts->rmin > 0.0) || !(opts->volfrac > 0.0 && opts->volfrac <= 1.0))
@@ -101,6 +102,7 @@ extern "C" int gbsimp_simp_run(gbsimp_ctx *ctx, int nx, int ny, int nz, const gb
     gbsimp_solve_stats sstats = {};
     const int64_t nd = 3LL * (nx + 1) * (ny + 1) * (nz + 1);
     for (; it < opts->n_iters; ++it) {
+        NvtxRange iteration("SIMP iteration");
         // u holds the last solution from the second iteration on, u_prev the one before from the
         // third on (the caller's initial u is not a solution of this loop)
         if (it >= 2) {

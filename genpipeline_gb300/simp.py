@@ -136,6 +136,25 @@ class SimpProblem:
         self.u_prev.copy_(u_prev)
         self.solved = solved
 
+    def save_state(self, path: str) -> None:
+        """Writes what the next iterations depend on to an .npz file: the design x, xPhys, the
+        displacements of the last two solves (the warm start) and the iteration counters. The
+        reference keeps a SIMP run's state in memory only (simp_solver_gpu.py:65,793); with
+        load_state a run can resume in another process and continue bit for bit."""
+        np.savez(path, x=self.x.cpu().numpy(), xphys=self.xphys.cpu().numpy(), u=self.u.cpu().numpy(),
+                 u_prev=self.u_prev.cpu().numpy(), solved=np.int64(self.solved),
+                 iteration=np.int64(self.iteration), grid=np.asarray(self.grid, dtype=np.int64))
+
+    def load_state(self, path: str) -> None:
+        """Restores a state written by save_state into this problem (same grid; the load case,
+        material and solve settings are this problem's own)."""
+        with np.load(path) as d:
+            if tuple(int(v) for v in d["grid"]) != self.grid:
+                raise ValueError(f"state of grid {tuple(d['grid'])} does not fit grid {self.grid}")
+            self.restore((torch.as_tensor(d["x"]), torch.as_tensor(d["xphys"]), torch.as_tensor(d["u"]),
+                          torch.as_tensor(d["u_prev"]), int(d["solved"])))
+            self.iteration = int(d["iteration"])
+
     def compliance(self) -> float:
         """f . u of the current displacement (synchronises)."""
         self.eng.dot64(self.f, self.u, out=self.comp)
