@@ -173,8 +173,10 @@ constexpr int kMaxStencil = 1024;
 struct Stencil {
     int n;
     int r;
+    int flat;              // 1: doff[] holds the flat offsets of this grid
     int off[kMaxStencil];  // dx, dy, dz packed as signed bytes
     float w[kMaxStencil];  // rmin - dist > 0
+    int doff[kMaxStencil]; // (dx ny + dy) nz + dz: the element offset in x-y-z order
 };
 
 // The neighbourhood of simp_solver.py:1553-1565: offsets of the box of half-width
@@ -184,6 +186,7 @@ static int make_stencil(double rmin, Stencil *s) {
     const int r = (int)ceil(rmin);
     s->n = 0;
     s->r = r;
+    s->flat = 0;
     for (int di = -r; di <= r; ++di)
         for (int dj = -r; dj <= r; ++dj)
             for (int dk = -r; dk <= r; ++dk) {
@@ -198,6 +201,19 @@ static int make_stencil(double rmin, Stencil *s) {
                 ++s->n;
             }
     return GBS_OK;
+}
+
+// The flat element offsets of the stencil for a grid of ny x nz element rows, when every
+// one fits in an int (s->flat = 1; otherwise the kernel uses the bounds-checked path only).
+static void set_flat_offsets(int ny, int nz, Stencil *s) {
+    const int64_t reach = (int64_t)s->r * ((int64_t)ny * nz + nz + 1);
+    s->flat = reach < INT32_MAX ? 1 : 0;
+    if (!s->flat) return;
+    for (int q = 0; q < s->n; ++q) {
+        const int o = s->off[q];
+        const int di = (int)(int8_t)(o & 0xff), dj = (int)(int8_t)((o >> 8) & 0xff), dk = (int)(int8_t)((o >> 16) & 0xff);
+        s->doff[q] = (int)(((int64_t)di * ny + dj) * nz + dk);
+    }
 }
 
 __device__ __forceinline__ void neumaier_add(float &s, float &c, float v) {
@@ -225,16 +241,31 @@ __global__ void __launch_bounds__(256) filter_kernel(int nx, int ny, int nz, con
         // FP32 with compensated (Neumaier) summation in the fixed stencil order: error of a
         // few ulp whatever the stencil size (up to ~900 terms at rmin 6).
         float s = 0.0f, sc = 0.0f, ws = 0.0f, wc = 0.0f;
-        for (int q = 0; q < st.n; ++q) {
-            int di, dj, dk;
-            unpack_off(st.off[q], di, dj, dk);
-            const int i2 = i + di, j2 = j + dj, k2 = k + dk;
-            if (i2 < 0 || i2 >= nx || j2 < 0 || j2 >= ny || k2 < 0 || k2 >= nz) continue;
-            const int64_t e2 = ((int64_t)i2 * ny + j2) * nz + k2;
-            const float w = st.w[q];
-            neumaier_add(ws, wc, w);
-            if (mode == 0) neumaier_add(s, sc, w * in[e2]);
-            else if (mode == 1) neumaier_add(s, sc, w * (in[e2] / hs[e2]));
+        // Away from the x and y faces only z can leave the grid: the same terms in the same
+        // order, with one z test and a precomputed flat offset per term (a warp's elements
+        // lie in one or two z columns, so the branch rarely splits a warp).
+        if (st.flat && i >= st.r && i < nx - st.r && j >= st.r && j < ny - st.r) {
+            for (int q = 0; q < st.n; ++q) {
+                const int k2 = k + (int)(int8_t)((st.off[q] >> 16) & 0xff);
+                if (k2 < 0 || k2 >= nz) continue;
+                const int64_t e2 = e + st.doff[q];
+                const float w = st.w[q];
+                neumaier_add(ws, wc, w);
+                if (mode == 0) neumaier_add(s, sc, w * in[e2]);
+                else if (mode == 1) neumaier_add(s, sc, w * (in[e2] / hs[e2]));
+            }
+        } else {
+            for (int q = 0; q < st.n; ++q) {
+                int di, dj, dk;
+                unpack_off(st.off[q], di, dj, dk);
+                const int i2 = i + di, j2 = j + dj, k2 = k + dk;
+                if (i2 < 0 || i2 >= nx || j2 < 0 || j2 >= ny || k2 < 0 || k2 >= nz) continue;
+                const int64_t e2 = ((int64_t)i2 * ny + j2) * nz + k2;
+                const float w = st.w[q];
+                neumaier_add(ws, wc, w);
+                if (mode == 0) neumaier_add(s, sc, w * in[e2]);
+                else if (mode == 1) neumaier_add(s, sc, w * (in[e2] / hs[e2]));
+            }
         }
         s += sc;
         ws += wc;
@@ -264,6 +295,7 @@ int filter_launch(const gbsimp_ctx *ctx, int nx, int ny, int nz, double rmin, in
     Stencil s;
     int rc = make_stencil(rmin, &s);
     if (rc) return rc;
+    set_flat_offsets(ny, nz, &s);
     const int64_t n = (int64_t)nx * ny * nz;
     filter_kernel<<<elem_blocks(ctx, n, 256), 256, 0, st>>>(nx, ny, nz, fast_div(ny), fast_div(nz), s, mode, hs, in,
                                                             preserved, out);
