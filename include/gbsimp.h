@@ -237,8 +237,8 @@ int gbsimp_time_pcg_apply(gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_
                           const float *x, const uint8_t *node_mask, int reps, void *ws,
                           size_t ws_bytes, double *seconds_per_launch, void *stream);
 /* FP32 PCG inner solves with outer defect correction: r = D(f - K u), FP32 PCG on K d = r
- * to inner_rtol, u += d (FP64), until ||r|| <= rtol ||D f||. u (FP64) holds the warm start on
- * entry. For rtol >= 1e-9 and a modal-form Ke, unless opts->residual_fp64 is set, the
+ * from d = 0 to max(inner_rtol, rtol / (||r|| / ||D f||)), u += d (FP64), until
+ * ||r|| <= rtol ||D f||. u (FP64) holds the warm start on entry. For rtol >= 1e-9 and a modal-form Ke, unless opts->residual_fp64 is set, the
  * residual runs in double-float arithmetic (FP32 pairs: rounding about 2^-46 of the
  * displacement magnitudes of an element, measured below 6.1e-13 ||D f|| on converged fields)
  * with FP64 u; otherwise its element products are FP64. Synchronises the stream. */
