@@ -141,9 +141,10 @@ class SimpProblem:
         displacements of the last two solves (the warm start) and the iteration counters. The
         reference keeps a SIMP run's state in memory only (simp_solver_gpu.py:65,793); with
         load_state a run can resume in another process and continue bit for bit."""
-        np.savez(path, x=self.x.cpu().numpy(), xphys=self.xphys.cpu().numpy(), u=self.u.cpu().numpy(),
-                 u_prev=self.u_prev.cpu().numpy(), solved=np.int64(self.solved),
-                 iteration=np.int64(self.iteration), grid=np.asarray(self.grid, dtype=np.int64))
+        with open(path, "wb") as fh:  # the file is `path` itself (np.savez would append .npz to a name)
+            np.savez(fh, x=self.x.cpu().numpy(), xphys=self.xphys.cpu().numpy(), u=self.u.cpu().numpy(),
+                     u_prev=self.u_prev.cpu().numpy(), solved=np.int64(self.solved),
+                     iteration=np.int64(self.iteration), grid=np.asarray(self.grid, dtype=np.int64))
 
     def load_state(self, path: str) -> None:
         """Restores a state written by save_state into this problem (same grid; the load case,

@@ -44,7 +44,7 @@ def test_save_state_resumes_bit_for_bit(tmp_path):
     a = SimpProblem(spec, f, fixed)
     for _ in range(4):
         a.step()
-    path = str(tmp_path / "simp_state.npz")
+    path = str(tmp_path / "simp_state")  # any name: the file is written under it as given
     a.save_state(path)
     b = SimpProblem(spec, f, fixed)
     b.load_state(path)
