@@ -1110,7 +1110,7 @@ struct ApplyProfile {
 int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *glaw, const float *x, const float *b,
             const uint8_t *mask, float *u, double rtol, int max_iter, int check_every, void *ws, PcgScalars *out,
             cudaStream_t st, ApplyProfile *prof = nullptr, int fused = 0, unsigned setup_flags = 0,
-            const float2 *bdd = nullptr, const double *bscale = nullptr) {
+            const float2 *bdd = nullptr, const double *bscale = nullptr, bool *finish_left = nullptr) {
     const int64_t nd = n_dof_of(nx, ny, nz);
     PcgWs w = pcg_ws(ws, nx, ny, nz);
     const Law<float> law = make_law<float>(*glaw);
@@ -1148,6 +1148,11 @@ int pcg_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *gla
         const int lrc = launch_loop_graph(ctx, nx, ny, nz, law, x, mask, u, w, st, &built);
         if (built) {
             if (lrc) return lrc;  // the launch itself failed
+            if (finish_left && async && use_modal(ctx, nz)) {
+                // the caller publishes, finalizes and applies the correction in one pass
+                *finish_left = true;
+                return GBS_OK;
+            }
             rc = cg_publish(ctx, nx, ny, nz, w, 1, st);
             if (rc) return rc;
             pcg_finalize_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, w.p0, w.p1, u, w.sc, use_modal(ctx, nz) ? 2 : 1);
@@ -1394,6 +1399,65 @@ __global__ void correct_dd_kernel(int64_t nd, const float *__restrict__ d, const
     }
 }
 
+// After a graph loop of one-kernel PCG launches that ended on launch parity `last`:
+// cg_fold_kernel, pcg_finalize_kernel (one-kernel form) and correct_dd_kernel in one pass.
+// Every block reads the state once and folds pending sums itself (the same totals in every
+// block); block 0 publishes the host-visible fields. No block writes the state slot, and the
+// done and status merges give the same value whether a block reads those fields before or after
+// block 0 has written them. Each DOF then takes x's owed half step (finalize) and
+// u += ||r|| x in FP64 with its split (correct).
+__global__ void cg_finish_dd_kernel(int64_t nd, int nblk, int last, const double *partials, PcgScalars *sc,
+                                    const float *__restrict__ p0, const float *__restrict__ xu,
+                                    const OuterScalars *os, const uint8_t *__restrict__ mask, double *u,
+                                    float2 *udd) {
+    __shared__ float2 sred[3 * 32];
+    __shared__ CgState s_state;
+    __shared__ int s_done, s_status;
+    __shared__ double s_bnorm;
+    if (threadIdx.x == 0) s_state = sc->st[last];
+    __syncthreads();
+    CgState s = s_state;
+    const int pend = s.pending;
+    if ((pend == CG_PENDING_STEP || pend == CG_PENDING_FIRST) && !s.done)  // block-uniform
+        cg_fold<256>(s, sc, (const float2 *)partials + last * 3 * nblk, nblk, sred);
+    if (threadIdx.x == 0) {
+        const int st0 = sc->status;
+        s_status = st0 == GBS_OK ? s.status : st0;
+        s_done = (sc->done || s.done) ? 1 : 0;
+        s_bnorm = pend == CG_PENDING_FIRST ? sqrt(df_value(s.rr)) : sc->bnorm;
+    }
+    __syncthreads();
+    const int status = s_status, done = s_done;
+    const double bnorm = s_bnorm;
+    const double a1 = df_value(s.done ? s.alpha : s.alpha_prev);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (pend == CG_PENDING_FIRST) sc->bnorm = bnorm;
+        sc->iter = s.iter;
+        sc->rz = df_value(s.gamma);
+        sc->rr = df_value(s.rr);
+        sc->pap = df_value(s.pap);
+        sc->alpha[0] = df_value(s.alpha);
+        sc->alpha[1] = a1;
+        sc->beta = df_value(s.beta);
+        sc->status = status;
+        sc->done = done;
+    }
+    // pcg_finalize_kernel, one-kernel form: x = 0 when D b = 0; when the last launched
+    // iteration was even (iter odd) x still owes alpha p of it
+    const bool zero = bnorm == 0.0;
+    const bool owe = done && !zero && (s.iter & 1) && status != GBS_ENONFINITE;
+    const float a = (float)a1;
+    const double rn = os->rnorm;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x) {
+        const float d = (done && zero) ? 0.0f : (owe ? fmaf(a, p0[i], xu[i]) : xu[i]);
+        const bool fx = dof_fixed(mask, i);
+        const double v = fx ? 0.0 : fma(f2d(d), rn, u[i]);
+        u[i] = v;
+        const ddv w = fx ? ddv{0.0f, 0.0f} : dd_split(v);
+        udd[i] = make_float2(w.h, w.l);
+    }
+}
+
 __global__ void scale_to_f32_kernel(int64_t nd, const double *__restrict__ r, const OuterScalars *os, float *b,
                                     float *d) {
     const double s = os->scale;
@@ -1557,11 +1621,15 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
         // Inner tolerance: enough to reach rtol from here, but not below what FP32 resolves.
         double itol = o->rtol / relres;
         if (itol < inner) itol = inner;
+        // with the double-float residual the graph loop's publish, finalize and the correction
+        // run as one pass (cg_finish_dd_kernel)
+        bool finish_left = false;
         {
             NvtxRange range("inner PCG");
             rc = pcg_run(ctx, nx, ny, nz, law, x, w.b32, mask, w.d32, itol, o->max_iter - total, o->check_every, w.pcg,
                          async ? nullptr : &ps, st, o->profile ? &prof : nullptr, o->fused, flags,
-                         scaled_in_start ? (const float2 *)w.r64 : nullptr, scaled_in_start ? &w.os->scale : nullptr);
+                         scaled_in_start ? (const float2 *)w.r64 : nullptr, scaled_in_start ? &w.os->scale : nullptr,
+                         dd ? &finish_left : nullptr);
         }
         if (rc) return rc;
         if (async) {
@@ -1573,8 +1641,16 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
                 if (ps.iter == 0) break;
             }
         }
-        rc = outer_correct(ctx, nd, mask, u, dd, w, st);
-        if (rc) return rc;
+        if (finish_left) {
+            const int nblk = modal_blocks<MODE_CG>(ctx, nx, ny, nz);
+            if (nblk < 0) return -nblk;
+            cg_finish_dd_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, nblk, 1, pw.partials, pw.sc, pw.p0, w.d32,
+                                                                    w.os, mask, u, w.udd);
+            GBS_LAUNCH_CHECK("cg_finish_dd_kernel");
+        } else {
+            rc = outer_correct(ctx, nd, mask, u, dd, w, st);
+            if (rc) return rc;
+        }
         if (status != GBS_OK) break;
     }
     if (stats) {
