@@ -1644,8 +1644,10 @@ int solve_run(const gbsimp_ctx *ctx, int nx, int ny, int nz, const gbsimp_law *l
         if (finish_left) {
             const int nblk = modal_blocks<MODE_CG>(ctx, nx, ny, nz);
             if (nblk < 0) return -nblk;
-            cg_finish_dd_kernel<<<ew_blocks(ctx, nd), 256, 0, st>>>(nd, nblk, 1, pw.partials, pw.sc, pw.p0, w.d32,
-                                                                    w.os, mask, u, w.udd);
+            // every block folds the ~300 partial sums itself: vec_blocks' cap (8 blocks per SM)
+            // keeps those redundant reads small
+            cg_finish_dd_kernel<<<vec_blocks(ctx, nd), 256, 0, st>>>(nd, nblk, 1, pw.partials, pw.sc, pw.p0, w.d32,
+                                                                     w.os, mask, u, w.udd);
             GBS_LAUNCH_CHECK("cg_finish_dd_kernel");
         } else {
             rc = outer_correct(ctx, nd, mask, u, dd, w, st);
