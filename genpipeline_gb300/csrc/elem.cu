@@ -612,7 +612,9 @@ __global__ void __launch_bounds__(kOcThreads) oc_coop_kernel(int64_t n, const Oc
         if (tid < kOcNodes) {
             double lo = s_l1, hi = s_l2;
             if (chain) {
-                for (int i = 0; i < tid; ++i) hi = 0.5 * (hi + lo);
+                // tid halvings 0.5 (hi + 0) of the all-left path: exact, so the same bits as that
+                // loop of dependent FP64 operations (l2 <= 1e9 stays far above the subnormals)
+                hi = ldexp(hi, -tid);
             } else {
                 const int path = tid + 1, depth = 31 - __clz(path);
                 for (int i = depth - 1; i >= 0; --i) {
@@ -687,19 +689,19 @@ __global__ void __launch_bounds__(kOcThreads) oc_coop_kernel(int64_t n, const Oc
         }
         __syncthreads();
         if (!s_ok) break;
-        // totals, the same way over the blocks' partials (loads issued four at a time)
+        // totals, the same way over the blocks' partials (loads issued eight at a time, added in
+        // block order)
         {
             df32 a{0.0f, 0.0f};
             if (t8 < kOcNodes) {
                 const float2 *pt = part + t8 * nblk;
                 int b = sub;
-                for (; b + 24 < nblk; b += 32) {
-                    const float2 p0 = __ldcg(&pt[b]), p1 = __ldcg(&pt[b + 8]), p2 = __ldcg(&pt[b + 16]),
-                                 p3 = __ldcg(&pt[b + 24]);
-                    a = df_add(a, df32{p0.x, p0.y});
-                    a = df_add(a, df32{p1.x, p1.y});
-                    a = df_add(a, df32{p2.x, p2.y});
-                    a = df_add(a, df32{p3.x, p3.y});
+                for (; b + 56 < nblk; b += 64) {
+                    float2 pv[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) pv[q] = __ldcg(&pt[b + 8 * q]);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) a = df_add(a, df32{pv[q].x, pv[q].y});
                 }
                 for (; b < nblk; b += 8) {
                     const float2 p = __ldcg(&pt[b]);
